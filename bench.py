@@ -1,0 +1,321 @@
+"""Throughput of the fused two-phase D2Q9 LBM step on GB300 (MLUPS).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--dtype f32|f64] [--impl ours|reference]
+
+Workload (the plain FP32 fused kernel at scale): a 4096 x 2048 lattice with
+walls at the bottom and top (the walled variant, fingering.py), Zou-He plug
+inlet u_x = 0.01 and the reference's velocity-type outlet, seeded random
+circular and square blocks with radius / half-side 6..14 placed to porosity
+0.7, tau_inv = 0.55, tau_def = 1.0, interfacial tension 5e-4, contact angle
+120 deg (psi_wall = cos 120 deg).  Synthetic, seeded; no dataset involved.
+
+A step is one iteration of the reference's loop body over the whole lattice
+(one fused kernel).  `value` is lattice updates per second over all ranks
+with the state resident in HBM (18 planes x 8.4 M cells x 4 B = 604 MB read
+and written per step, far larger than L2, so no L2 flush is needed).  `e2e`
+is the same metric through the host-buffer API: every step uploads the
+populations from pinned host memory, advances one iteration and downloads
+them again.  With --gpus N > 1 each rank runs its own instance (replicas,
+weak scaling, no collective on the data path).
+
+--impl reference times the CPU implementation of the same step (the numpy
+oracle, which restates the reference's numpy code operation for operation)
+on the host cores: one process per core, each on a 512 x 256 sample of the
+same generator.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+H_FULL, W_FULL = 2048, 4096
+SAMPLE_H, SAMPLE_W = 256, 512
+BYTES_PER_POP = {"f32": 4, "f64": 8}
+WORKLOAD = "walls_4096x2048_porosity0.7_blocks6-14"
+
+
+def workload(H, W, seed=2024):
+    from fingering_dynamics_gb300 import geometry as geo
+    from fingering_dynamics_gb300.params import from_relaxation_times
+    prm = from_relaxation_times(H, W, tau_inv=0.55, tau_def=1.0, sigma=5e-4, contact_angle_deg=120.0,
+                                u_in=0.01, variant="walls")
+    rects, circles = geo.random_blocks(H, W, 0.7, 6, 14, seed=seed, x_margin=32)
+    g = geo.build_geometry(H, W, rects=rects, circles=circles, walls=True)
+    return prm, g
+
+
+def measured_peak():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(key):
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh).get(key)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU (oracle) timing
+# ---------------------------------------------------------------------------
+def _cpu_sample_worker(args):
+    seed, iters, warm = args
+    import warnings
+    warnings.filterwarnings("ignore")
+    from oracle.lbm_oracle import OracleParams, OracleState
+    prm, g = workload(SAMPLE_H, SAMPLE_W, seed=seed)
+    op = OracleParams(H=prm.H, W=prm.W, variant="walls", tau=prm.tau, eta_n=prm.eta_n, M=prm.M, a=prm.a,
+                      kappa=prm.kappa, gamma=prm.gamma, psi_wall=prm.psi_wall, inlet_ux=prm.inlet_ux,
+                      outlet_coef=prm.outlet_coef)
+    st = OracleState(op, g.solid, prm.initial_psi(g.solid), init_mu=True, init_uy=True)
+    for _ in range(warm):
+        st.step(g.corner_list, g.circle_masks)
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        st.step(g.corner_list, g.circle_masks)
+    t1 = time.perf_counter()
+    return t0, t1, iters * prm.H * prm.W
+
+
+def cpu_baseline(max_seconds=15.0):
+    """One core, the oracle on a 512 x 256 sample, until ~max_seconds."""
+    import warnings
+    warnings.filterwarnings("ignore")
+    from oracle.lbm_oracle import OracleParams, OracleState
+    prm, g = workload(SAMPLE_H, SAMPLE_W)
+    op = OracleParams(H=prm.H, W=prm.W, variant="walls", tau=prm.tau, eta_n=prm.eta_n, M=prm.M, a=prm.a,
+                      kappa=prm.kappa, gamma=prm.gamma, psi_wall=prm.psi_wall, inlet_ux=prm.inlet_ux,
+                      outlet_coef=prm.outlet_coef)
+    st = OracleState(op, g.solid, prm.initial_psi(g.solid), init_mu=True, init_uy=True)
+    st.step(g.corner_list, g.circle_masks)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < max_seconds and n < 400:
+        st.step(g.corner_list, g.circle_masks)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": round(n * prm.H * prm.W / dt / 1e6, 4), "unit": "MLUPS", "cores": 1, "kind": "port",
+            "sample": f"numpy oracle, {SAMPLE_W}x{SAMPLE_H} lattice of the same generator, {n} steps in {dt:.1f} s, "
+                      f"1 process"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    iters = max(1, args.steps)
+    ctx = mp.get_context("spawn")
+    t_start = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_sample_worker, [(1000 + i, iters, max(1, args.warmup)) for i in range(cores)])
+    t0 = min(r[0] for r in res)
+    t1 = max(r[1] for r in res)
+    cells = sum(r[2] for r in res)
+    mlups = cells / (t1 - t0) / 1e6
+    ms = (t1 - t0) / iters * 1e3
+    sample = (f"numpy oracle (the reference's numpy step restated op for op), {cores} processes x "
+              f"{SAMPLE_W}x{SAMPLE_H} samples of the same generator, {iters} timed steps each")
+    line = {"metric": "MLUPS", "value": round(mlups, 4), "unit": "MLUPS", "n_gpus": args.gpus, "steps": iters,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": f"{SAMPLE_W}x{SAMPLE_H}", "variant": "walls"},
+            "cpu_baseline": {"value": round(mlups, 4), "unit": "MLUPS", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(mlups, 4), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": round(time.perf_counter() - t_start, 1)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU timing
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    from fingering_dynamics_gb300 import build
+    from fingering_dynamics_gb300.lattice import Lattice
+    build.build()
+    prm, g = workload(H_FULL, W_FULL, seed=2024 + rank)
+    lat = Lattice(prm, g, dtype=args.dtype, device=f"cuda:{local}")
+    H, W = prm.H, prm.W
+    lat.enter_fused()
+    for _ in range(args.warmup):
+        lat.advance(1, args.rows)
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            lat.advance(1, args.rows)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms_total = e0.elapsed_time(e1)
+    clocks = clk.summary()
+    finite = bool(torch.isfinite(lat.pop[lat.cur]).all().item())
+
+    # end to end through the host-buffer API: populations in from pinned host
+    # memory, one iteration, populations back out
+    host = torch.empty((18, H, W), dtype=lat.tdtype, pin_memory=True)
+    host.copy_(lat.pop[lat.cur])
+    e2e_steps = max(3, min(args.steps, 20))
+    for _ in range(2):
+        lat.upload_populations(host)
+        lat.advance(1, args.rows)
+        lat.download_populations(host)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        lat.upload_populations(host)
+        lat.advance(1, args.rows)
+        lat.download_populations(host)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+
+    t = torch.tensor([ms_total, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_total, e2e_s = float(t[0]), float(t[1])
+    if rank == 0:
+        nbytes = BYTES_PER_POP[args.dtype]
+        ms_step = ms_total / args.steps
+        cells = H * W
+        mlups = world * cells * args.steps / (ms_total / 1e3) / 1e6
+        alg_bytes = 36 * nbytes * cells
+        achieved = alg_bytes / (ms_step / 1e3) / 1e9
+        peak, peak_kind = measured_peak()
+        pop_bytes = 18 * cells * nbytes
+        line = {
+            "metric": "MLUPS", "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+            "config": {"workload": WORKLOAD, "H": H, "W": W, "variant": "walls", "porosity": round(g.porosity, 4),
+                       "blocks": len(g.rects) + len(g.circles),
+                       "tau_inv": 0.55, "tau_def": 1.0, "sigma": 5e-4, "contact_angle_deg": 120, "u_in": 0.01,
+                       "l2": "inputs larger than L2 (populations 2 x %d MB)" % (pop_bytes // 2 ** 20),
+                       "parallelism": f"replicas{world}", "rows_per_warp": args.rows or "auto",
+                       "state_finite_after_timing": finite},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "traffic": committed_traffic(f"fused_{args.dtype}_{W}x{H}"),
+                         "algorithmic_bytes_per_launch": alg_bytes},
+            "e2e": {"value": round(world * cells * e2e_steps / e2e_s / 1e6, 1), "unit": "MLUPS",
+                    "h2d_bytes_per_step": pop_bytes, "d2h_bytes_per_step": pop_bytes},
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--rows", type=int, default=0, help="rows per warp (0 = automatic)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

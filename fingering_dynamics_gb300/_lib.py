@@ -1,0 +1,94 @@
+"""ctypes binding of ``libfdlbm.so`` (the C ABI declared in include/fdlbm.h).
+
+There is no fallback: if the shared library is missing or fails to load,
+:func:`lib` raises.  Build it with ``python -m fingering_dynamics_gb300.build``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_lib", "libfdlbm.so")
+
+FD_OK = 0
+FD_F64, FD_F32, FD_F16, FD_BF16 = 0, 1, 2, 3
+FD_VARIANT_PERIODIC, FD_VARIANT_WALLS = 0, 1
+FD_INIT_MU, FD_INIT_UY = 1, 2
+TERMS = {"large_F": 0, "feq": 1, "geq": 2, "F": 3, "G": 4}
+FIELDS = {"rho": 0, "npx": 1, "npy": 2, "np2": 3, "mu": 4, "mu_plain": 5, "ux": 6, "uy": 7, "p": 8, "mix_tau": 9}
+ERRORS = {-1: "FD_ERR_ARG", -2: "FD_ERR_SHAPE", -3: "FD_ERR_CUDA", -4: "FD_ERR_DTYPE", -5: "FD_ERR_SCRATCH"}
+
+
+class FDError(RuntimeError):
+    """A libfdlbm call returned a negative status."""
+
+    def __init__(self, code, fn, msg):
+        super().__init__(f"{fn}: {ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class fd_params(C.Structure):
+    _fields_ = [("H", C.c_int32), ("W", C.c_int32), ("variant", C.c_int32), ("flags", C.c_uint32),
+                ("tau", C.c_double), ("eta_n", C.c_double), ("M", C.c_double), ("a", C.c_double),
+                ("kappa", C.c_double), ("gamma", C.c_double), ("psi_wall", C.c_double),
+                ("outlet_coef", C.c_double)]
+
+
+class fd_fields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("f", "g", "psi", "npx", "npy", "np2", "rho", "ux", "uy", "p", "mu",
+                                          "mix_tau")]
+
+
+_VP, _I, _PD = C.c_void_p, C.c_int, C.c_ssize_t
+_P = C.POINTER(fd_params)
+_F = C.POINTER(fd_fields)
+
+# name -> argtypes (all return int status unless listed in _RET)
+SIGNATURES = {
+    "fd_abi_version": [],
+    "fd_last_error": [],
+    "fd_compute_init": [_P, _I, _VP, _VP, _VP, _F, _VP],
+    "fd_collide": [_P, _I, _VP, _F, _VP],
+    "fd_collision_term": [_P, _I, _I, _I, _VP, _F, _VP, _VP],
+    "fd_stream": [_P, _I, _VP, _VP, _VP, _VP, _VP],
+    "fd_bounce_back": [_P, _I, _VP, _VP, _VP, _VP, _VP, _VP],
+    "fd_bottom_top_wall": [_I, _I, _I, _PD, _PD, _VP, _VP, _VP, _VP, _VP],
+    "fd_boundary_fields": [_P, _I, _VP, _VP, _VP, _VP, _VP],
+    "fd_zou_he_inlet": [_P, _I, _VP, _VP, _VP, _VP, _VP],
+    "fd_zou_he_outlet": [_P, _I, _VP, _VP, _VP, _VP, _VP],
+    "fd_update_rho_psi": [_P, _I, _VP, _F, _VP],
+    "fd_update_macros": [_P, _I, _VP, _F, _VP],
+    "fd_field": [_P, _I, _I, _VP, _F, _VP, _VP],
+    "fd_fused_step": [_P, _I, _VP, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
+}
+_RET = {"fd_last_error": C.c_char_p}
+
+_lock = threading.Lock()
+_handle = None
+
+
+def lib():
+    """Load (once) and return the bound library.  Raises if it is missing."""
+    global _handle
+    with _lock:
+        if _handle is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"libfdlbm.so not built ({LIB_PATH}); run python -m fingering_dynamics_gb300.build")
+            h = C.CDLL(LIB_PATH)
+            for name, args in SIGNATURES.items():
+                fn = getattr(h, name)
+                fn.argtypes = args
+                fn.restype = _RET.get(name, C.c_int)
+            _handle = h
+        return _handle
+
+
+def call(name, *args):
+    """Call an entry point and raise FDError on a negative status."""
+    h = lib()
+    r = getattr(h, name)(*args)
+    if r != FD_OK:
+        raise FDError(r, name, h.fd_last_error().decode(errors="replace"))
+    return r

@@ -1,0 +1,45 @@
+// Host-side helpers shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+
+#include "../../include/fdlbm.h"
+
+namespace fd {
+
+// Message of the last failing call on this host thread (fd_last_error).
+void set_error(const char* fmt, ...);
+
+#define FD_REQUIRE(cond, code, ...)  \
+  do {                               \
+    if (!(cond)) {                   \
+      ::fd::set_error(__VA_ARGS__);  \
+      return (code);                 \
+    }                                \
+  } while (0)
+
+inline int check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return FD_ERR_CUDA;
+  }
+  return FD_OK;
+}
+
+inline int check_params(const fd_params* p) {
+  FD_REQUIRE(p != nullptr, FD_ERR_ARG, "params is NULL");
+  FD_REQUIRE(p->H >= 2 && p->W >= 2, FD_ERR_SHAPE, "lattice %dx%d too small", p->H, p->W);
+  FD_REQUIRE(p->variant == FD_VARIANT_PERIODIC || p->variant == FD_VARIANT_WALLS, FD_ERR_ARG,
+             "unknown variant %d", p->variant);
+  FD_REQUIRE(p->variant != FD_VARIANT_WALLS || p->H >= 3, FD_ERR_SHAPE,
+             "the walled variant needs H >= 3 (walls act on rows 1 and H-2)");
+  return FD_OK;
+}
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+}  // namespace fd

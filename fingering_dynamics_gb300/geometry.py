@@ -355,6 +355,8 @@ class Geometry:
     corner_list: list = field(default_factory=list)
     circle_masks: tuple | None = None   # (side_list, concave_list, convex_list)
     walls: bool = False
+    rects: list = field(default_factory=list)     # ((x0, y0), (x1, y1)) as given
+    circles: list = field(default_factory=list)   # ((cx, cy), r) as given
 
     @property
     def fluid(self) -> np.ndarray:
@@ -385,7 +387,8 @@ def build_geometry(H: int, W: int, rects=(), circles=(), walls: bool = False) ->
     if walls:
         links.append(wall_row_link_bits(H, W))
     solid = bpa == 1
-    return Geometry(H, W, bpa, solid, pack_mask(solid, *links), corner_list, circle_masks, walls)
+    return Geometry(H, W, bpa, solid, pack_mask(solid, *links), corner_list, circle_masks, walls,
+                    list(rects), list(circles))
 
 
 def random_blocks(H: int, W: int, porosity: float, rmin: int, rmax: int, seed: int,

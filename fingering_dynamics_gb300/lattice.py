@@ -1,0 +1,219 @@
+"""GPU lattice state and stepping.
+
+:class:`Lattice` owns one simulation's device buffers and drives the CUDA
+kernels through the C ABI.  It offers two equivalent ways to advance:
+
+* :meth:`Lattice.step_reference` runs the reference's loop body
+  (fingering_periodic.py:454-479 / fingering.py:558-585) one function at a
+  time, each function one kernel.
+* :meth:`Lattice.step` / :meth:`Lattice.advance` use the fused kernel, one
+  launch per iteration.
+
+Device layout (all torch tensors on one GPU):
+
+* ``pop[0]``, ``pop[1]``: (18, H, W) population buffers, f planes then g
+  planes.  In *reference* mode ``pop[cur]`` holds the pre-collision
+  populations of the current iteration (the reference's ``f``/``g``); in
+  *fused* mode it holds the post-collision populations whose streaming is
+  pending.  Switching modes costs one collision or one
+  stream + bounce-back + Zou-He + macroscopic update; no buffer is copied.
+* ``side[0]``, ``side[1]``: (6, H) psi_x, psi_y, mu at columns 0 and W-1.
+* ``psi``, ``npx``, ``npy``, ``np2``, ``rho``, ``ux``, ``uy``, ``p``, ``mu``,
+  ``mix_tau``: (H, W) fields, current in reference mode.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .geometry import Geometry
+from .params import LBMParams
+
+DTYPES = {"f64": (torch.float64, L.FD_F64), "f32": (torch.float32, L.FD_F32)}
+FIELD_NAMES = ("psi", "npx", "npy", "np2", "rho", "ux", "uy", "p", "mu", "mix_tau")
+
+
+def make_fd_params(prm: LBMParams) -> L.fd_params:
+    flags = (L.FD_INIT_MU if prm.init_mu else 0) | (L.FD_INIT_UY if prm.init_uy else 0)
+    return L.fd_params(prm.H, prm.W, prm.variant_id, flags, prm.tau, prm.eta_n, prm.M, prm.a, prm.kappa,
+                       prm.gamma, prm.psi_wall, prm.outlet_coef)
+
+
+def _ptr(t: torch.Tensor | None):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+class Lattice:
+    """One two-phase D2Q9 simulation resident on a GPU."""
+
+    def __init__(self, params: LBMParams, geometry: Geometry, dtype: str = "f64", device="cuda",
+                 rho0: np.ndarray | None = None, psi0: np.ndarray | None = None):
+        if dtype not in DTYPES:
+            raise ValueError(f"dtype must be one of {sorted(DTYPES)}")
+        if (geometry.H, geometry.W) != (params.H, params.W):
+            raise ValueError("geometry and params disagree on the lattice size")
+        self.params = params
+        self.geometry = geometry
+        self.dtype = dtype
+        self.tdtype, self.fd_dtype = DTYPES[dtype]
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("Lattice runs on a CUDA device only")
+        H, W = params.H, params.W
+        self.H, self.W = H, W
+        self.prm = make_fd_params(params)
+        dev, td = self.device, self.tdtype
+        self.mask = torch.from_numpy(np.ascontiguousarray(geometry.mask_word).view(np.int16)).to(dev)
+        self.fluid = torch.from_numpy(~geometry.solid).to(dev)
+        self.inlet_ux = torch.from_numpy(np.ascontiguousarray(params.inlet_ux, np.float64)).to(dev)
+        self.pop = [torch.zeros((18, H, W), dtype=td, device=dev) for _ in range(2)]
+        self.side = [torch.zeros((6, H), dtype=td, device=dev) for _ in range(2)]
+        self.cur = 0
+        self.scur = 0
+        for n in FIELD_NAMES:
+            setattr(self, n, torch.zeros((H, W), dtype=td, device=dev))
+        psi0 = params.initial_psi(geometry.solid) if psi0 is None else np.asarray(psi0, np.float64)
+        psi0_d = torch.from_numpy(np.ascontiguousarray(psi0, np.float64)).to(dev)
+        rho0_d = None if rho0 is None else torch.from_numpy(np.ascontiguousarray(rho0, np.float64)).to(dev)
+        self.mode = "reference"
+        self.iteration = 0
+        L.call("fd_compute_init", C.byref(self.prm), self.fd_dtype, _ptr(self.mask), _ptr(psi0_d), _ptr(rho0_d),
+               C.byref(self.fields()), self._stream())
+        self._keep = (psi0_d, rho0_d)  # alive until the init kernels ran
+        torch.cuda.current_stream(self.device).synchronize()
+        self._keep = None
+
+    # ------------------------------------------------------------------
+    @property
+    def f(self) -> torch.Tensor:
+        return self.pop[self.cur][:9]
+
+    @property
+    def g(self) -> torch.Tensor:
+        return self.pop[self.cur][9:]
+
+    def _stream(self):
+        return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def fields(self, pop: torch.Tensor | None = None) -> L.fd_fields:
+        p = self.pop[self.cur] if pop is None else pop
+        return L.fd_fields(p.data_ptr(), p[9:].data_ptr(), *(getattr(self, n).data_ptr() for n in
+                                                              ("psi", "npx", "npy", "np2", "rho", "ux", "uy", "p",
+                                                               "mu", "mix_tau")))
+
+    # ------------------------------------------------------------------
+    # reference-order pieces (each one kernel)
+    # ------------------------------------------------------------------
+    def _require(self, mode):
+        if self.mode != mode:
+            raise RuntimeError(f"lattice is in {self.mode} mode, this call needs {mode} mode")
+
+    def collide(self):
+        """fingering_periodic.py:455-460 in place on the current populations."""
+        self._require("reference")
+        L.call("fd_collide", C.byref(self.prm), self.fd_dtype, _ptr(self.mask), C.byref(self.fields()), self._stream())
+
+    def boundary_fields(self, out: torch.Tensor):
+        L.call("fd_boundary_fields", C.byref(self.prm), self.fd_dtype, _ptr(self.mask), _ptr(self.psi), _ptr(self.np2),
+               _ptr(out), self._stream())
+
+    def _finish_from(self, src: torch.Tensor, side: torch.Tensor, dst: torch.Tensor):
+        """stream + bounce-back + Zou-He + macroscopic update of a pending
+        iteration: ``src`` holds post-collision populations (also the
+        reference's f_behind snapshot), ``dst`` receives the new ones."""
+        s = self._stream()
+        prm = C.byref(self.prm)
+        L.call("fd_stream", prm, self.fd_dtype, _ptr(src), _ptr(src[9:]), _ptr(dst), _ptr(dst[9:]), s)
+        L.call("fd_bounce_back", prm, self.fd_dtype, _ptr(self.mask), _ptr(src), _ptr(src[9:]), _ptr(dst),
+               _ptr(dst[9:]), s)
+        L.call("fd_zou_he_inlet", prm, self.fd_dtype, _ptr(dst), _ptr(dst[9:]), _ptr(side), _ptr(self.inlet_ux), s)
+        L.call("fd_zou_he_outlet", prm, self.fd_dtype, _ptr(dst), _ptr(dst[9:]), _ptr(side), _ptr(self.inlet_ux), s)
+        fl = C.byref(self.fields(dst))
+        L.call("fd_update_rho_psi", prm, self.fd_dtype, _ptr(self.mask), fl, s)
+        L.call("fd_update_macros", prm, self.fd_dtype, _ptr(self.mask), fl, s)
+
+    def step_reference(self, n: int = 1):
+        """n iterations of the loop body, one kernel per reference function."""
+        self._require("reference")
+        for _ in range(n):
+            self.collide()
+            self.boundary_fields(self.side[self.scur])
+            src, dst = self.pop[self.cur], self.pop[1 - self.cur]
+            self._finish_from(src, self.side[self.scur], dst)
+            self.cur = 1 - self.cur
+            self.iteration += 1
+
+    # ------------------------------------------------------------------
+    # fused path
+    # ------------------------------------------------------------------
+    def enter_fused(self):
+        """Collide the current iteration and keep the result as fused state."""
+        if self.mode == "fused":
+            return
+        self.boundary_fields(self.side[self.scur])
+        self.collide()
+        self.mode = "fused"
+
+    def advance(self, n: int, rows_per_warp: int = 0):
+        """n fused kernels (n more collisions); stays in fused mode."""
+        self._require("fused")
+        if n <= 0:
+            return
+        a, b = self.pop[self.cur], self.pop[1 - self.cur]
+        sa, sb = self.side[self.scur], self.side[1 - self.scur]
+        L.call("fd_fused_step", C.byref(self.prm), self.fd_dtype, _ptr(self.mask), _ptr(self.inlet_ux), _ptr(a),
+               _ptr(b), _ptr(sa), _ptr(sb), int(n), int(rows_per_warp), self._stream())
+        if n % 2:
+            self.cur = 1 - self.cur
+            self.scur = 1 - self.scur
+        self.iteration += n
+
+    def exit_fused(self):
+        """Finish the pending iteration; the fields become current."""
+        if self.mode == "reference":
+            return
+        src, dst = self.pop[self.cur], self.pop[1 - self.cur]
+        self._finish_from(src, self.side[self.scur], dst)
+        self.cur = 1 - self.cur
+        self.mode = "reference"
+        self.iteration += 1
+
+    def step(self, n: int = 1, rows_per_warp: int = 0):
+        """n iterations of the loop body through the fused kernel."""
+        if n <= 0:
+            return
+        if self.mode == "reference":
+            self.enter_fused()
+            self.advance(n - 1, rows_per_warp)
+            self.exit_fused()
+        else:
+            self.advance(n, rows_per_warp)
+
+    # ------------------------------------------------------------------
+    # host buffers
+    # ------------------------------------------------------------------
+    def upload_populations(self, host: torch.Tensor):
+        """Copy (18, H, W) populations from host memory into the current
+        buffer (asynchronous when ``host`` is pinned)."""
+        self.pop[self.cur].copy_(host, non_blocking=True)
+
+    def download_populations(self, host: torch.Tensor):
+        """Copy the current (18, H, W) populations into host memory."""
+        host.copy_(self.pop[self.cur], non_blocking=True)
+
+    # ------------------------------------------------------------------
+    def state(self) -> dict:
+        """Host copies of the reference-layout state (reference mode)."""
+        self._require("reference")
+        torch.cuda.current_stream(self.device).synchronize()
+        out = {"f": self.f.double().cpu().numpy(), "g": self.g.double().cpu().numpy()}
+        solid = self.geometry.solid
+        for n in FIELD_NAMES:
+            a = getattr(self, n).double().cpu().numpy()
+            if n in ("rho", "ux", "uy", "p", "mu", "mix_tau"):
+                a = np.where(solid, np.nan, a)
+            out[n] = a
+        return out

@@ -1,0 +1,200 @@
+/*
+ * fdlbm - C ABI of the GB300 (sm_103a) two-phase D2Q9 lattice-Boltzmann step.
+ *
+ * The entry points replace, one for one, the step and boundary functions of
+ * the reference scripts lattice_boltzmann/fingering_periodic.py (periodic in
+ * y) and lattice_boltzmann/fingering.py (walls at bottom and top), plus
+ * bounce_back.py.  Each declaration names the reference code it replaces.
+ *
+ * Conventions
+ *   - All array arguments are DEVICE pointers unless stated otherwise; the
+ *     caller owns every buffer (torch tensors, cudaMalloc, ...).
+ *   - Populations are (9, H, W) direction-major, row-major planes; fields are
+ *     (H, W) row-major; the element type is given by `dtype`.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     asynchronous; errors detected on the host are returned immediately,
+ *     launch errors are returned from the call that launched.
+ *   - Every call returns FD_OK (0) or a negative FD_ERR_* code;
+ *     fd_last_error() gives the message of the last failure on the calling
+ *     host thread.
+ *   - Macroscopic fields are stored on the full (H, W) grid; values on solid
+ *     cells are not defined (the reference keeps them as 1-D arrays over fluid
+ *     cells, fingering_periodic.py:103-113).
+ */
+#ifndef FDLBM_H
+#define FDLBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDLBM_ABI_VERSION 1
+
+enum fd_status {
+  FD_OK = 0,
+  FD_ERR_ARG = -1,      /* null pointer, bad enum, bad size */
+  FD_ERR_SHAPE = -2,    /* lattice shape not supported by this entry point */
+  FD_ERR_CUDA = -3,     /* CUDA launch or runtime error */
+  FD_ERR_DTYPE = -4,    /* dtype not supported by this entry point */
+  FD_ERR_SCRATCH = -5   /* request larger than a fixed scratch area */
+};
+
+enum fd_dtype { FD_F64 = 0, FD_F32 = 1, FD_F16 = 2, FD_BF16 = 3 };
+
+enum fd_variant {
+  FD_VARIANT_PERIODIC = 0, /* fingering_periodic.py: y periodic, Gaussian inlet, outlet 2/3 */
+  FD_VARIANT_WALLS = 1     /* fingering.py: psi_wall ghost rows, walls on rows 1 and H-2, corners, outlet 1.5 */
+};
+
+/* fd_params.flags */
+#define FD_INIT_MU 1u /* Compute.__init__ evaluates mu before the equilibria (fingering.py:122) */
+#define FD_INIT_UY 2u /* ... and u_y with f = 0 (fingering.py:123) */
+
+/* Model constants, the reference's module globals (fingering_periodic.py:15-44). */
+typedef struct fd_params {
+  int32_t H, W;
+  int32_t variant;     /* enum fd_variant */
+  uint32_t flags;      /* FD_INIT_* */
+  double tau;          /* g relaxation time */
+  double eta_n;        /* Eta_n */
+  double M;            /* viscosity ratio */
+  double a, kappa;     /* free-energy coefficients */
+  double gamma;        /* mobility */
+  double psi_wall;     /* psi on solid cells */
+  double outlet_coef;  /* 2/3 (fingering_periodic.py:317) or 1.5 (fingering.py:378) */
+} fd_params;
+
+/* Device pointers of the reference's Compute attributes (fingering_periodic.py:90-121). */
+typedef struct fd_fields {
+  void* f;        /* (9,H,W) */
+  void* g;        /* (9,H,W) */
+  void* psi;      /* (H,W) order parameter, psi_wall on solid */
+  void* npx;      /* (H,W) nabla_psix */
+  void* npy;      /* (H,W) nabla_psiy */
+  void* np2;      /* (H,W) nabla_psi2 */
+  void* rho;      /* (H,W) */
+  void* ux;       /* (H,W) */
+  void* uy;       /* (H,W) */
+  void* p;        /* (H,W) */
+  void* mu;       /* (H,W) */
+  void* mix_tau;  /* (H,W) */
+} fd_fields;
+
+/* Selector of fd_collision_term (fingering_periodic.py:194-199, 171-192, 258-264). */
+enum fd_term { FD_TERM_LARGE_F = 0, FD_TERM_FEQ = 1, FD_TERM_GEQ = 2, FD_TERM_F = 3, FD_TERM_G = 4 };
+
+/* Selector of fd_field (fingering_periodic.py:123-256). */
+enum fd_field_id {
+  FD_FIELD_RHO = 0,      /* getRho       fingering_periodic.py:151 */
+  FD_FIELD_NPX = 1,      /* getNabla_psix fingering_periodic.py:214 */
+  FD_FIELD_NPY = 2,      /* getNabla_psiy fingering_periodic.py:228 */
+  FD_FIELD_NP2 = 3,      /* getNabla_psi2 fingering_periodic.py:242 */
+  FD_FIELD_MU = 4,       /* getMu        fingering_periodic.py:141 */
+  FD_FIELD_MU_PLAIN = 5, /* getMu_plain  fingering_periodic.py:146 */
+  FD_FIELD_UX = 6,       /* getUx        fingering_periodic.py:126 */
+  FD_FIELD_UY = 7,       /* getUy        fingering_periodic.py:134 */
+  FD_FIELD_P = 8,        /* getP         fingering_periodic.py:123 */
+  FD_FIELD_MIX_TAU = 9   /* getMix_tau   fingering_periodic.py:201 */
+};
+
+/* ---- library ------------------------------------------------------------ */
+int fd_abi_version(void);
+const char* fd_last_error(void);
+
+/* ---- reference-order step, one entry per reference function (FP64 / FP32) -- */
+
+/* Compute.__init__ (fingering_periodic.py:48-121; fingering.py:54-127).
+ * psi0: (H,W) double initial psi before solid cells are set to psi_wall;
+ * rho0: (H,W) double initial density or NULL for 1.0.  Writes every member of
+ * `out`; populations on solid cells are zero. */
+int fd_compute_init(const fd_params* prm, int dtype, const uint16_t* mask, const double* psi0,
+                    const double* rho0, const fd_fields* out, void* stream);
+
+/* The collision loop body for all nine directions, fluid cells only:
+ * f[j][mask] = getF(j), g[j][mask] = getG(j) with F, feq, geq from the stored
+ * fields (fingering_periodic.py:455-460). In place on fields->f, fields->g. */
+int fd_collide(const fd_params* prm, int dtype, const uint16_t* mask, const fd_fields* fields, void* stream);
+
+/* One of getLarge_F(j), getfeq(j), getgeq(j), getF(j), getG(j)
+ * (fingering_periodic.py:194-199, 171-181, 183-192, 258-260, 262-264) on the
+ * full grid; `out` is (H,W) and is written on fluid cells only. */
+int fd_collision_term(const fd_params* prm, int dtype, int term, int j, const uint16_t* mask,
+                      const fd_fields* fields, void* out, void* stream);
+
+/* stream(f, g) (fingering_periodic.py:327-343): dst = src shifted by e_i,
+ * periodic in x and y, every cell.  src and dst must not overlap. */
+int fd_stream(const fd_params* prm, int dtype, const void* src_f, const void* src_g, void* dst_f,
+              void* dst_g, void* stream);
+
+/* Bounce_back.halfway_bounceback_rec / halfway_bounceback_circle
+ * (bounce_back.py:25-86, 89-167) and the wall rows of bottom_top_wall as
+ * called by fingering.py:573, expressed as link bits of `mask`:
+ * f_i(x) = f_behind_opp(i)(x) wherever bit i-1 of mask(x) is set. */
+int fd_bounce_back(const fd_params* prm, int dtype, const uint16_t* mask, const void* f_behind,
+                   const void* g_behind, void* f, void* g, void* stream);
+
+/* bottom_top_wall(f_behind, g_behind, f, g) (fingering.py:432-451) on
+ * arbitrary (9, rows, cols) views: row 0 of the view takes populations
+ * 2,5,6 from 4,7,8 of f_behind, row rows-1 takes 4,7,8 from 2,5,6.
+ * Strides are in elements. */
+int fd_bottom_top_wall(int dtype, int rows, int cols, ptrdiff_t plane_stride, ptrdiff_t row_stride,
+                       const void* f_behind, const void* g_behind, void* f, void* g, void* stream);
+
+/* The psi_x, psi_y, mu_plain values zou_he_boundary_inlet/outlet recompute
+ * from the stored psi and nabla_psi2 (fingering_periodic.py:273-275, 309-311),
+ * at columns 0 and W-1: side = 6 x H values of dtype
+ * [gx0, gy0, mu0, gxW, gyW, muW]. */
+int fd_boundary_fields(const fd_params* prm, int dtype, const uint16_t* mask, const void* psi,
+                       const void* np2, void* side, void* stream);
+
+/* zou_he_boundary_inlet (fingering_periodic.py:268-302; fingering.py:298-364).
+ * inlet_ux: (H) double u_x per row. */
+int fd_zou_he_inlet(const fd_params* prm, int dtype, void* f, void* g, const void* side,
+                    const double* inlet_ux, void* stream);
+
+/* zou_he_boundary_outlet (fingering_periodic.py:305-324; fingering.py:369-390). */
+int fd_zou_he_outlet(const fd_params* prm, int dtype, void* f, void* g, const void* side,
+                     const double* inlet_ux, void* stream);
+
+/* udpatePsi (fingering_periodic.py:210-212) into fields->psi, and
+ * getRho (fingering_periodic.py:151-152) into fields->rho. */
+int fd_update_rho_psi(const fd_params* prm, int dtype, const uint16_t* mask, const fd_fields* fields,
+                      void* stream);
+
+/* The macroscopic tail of the loop body (fingering_periodic.py:472-479):
+ * nabla_psix/psiy/psi2 from psi, then mu, ux, uy, p, mix_tau on fluid cells. */
+int fd_update_macros(const fd_params* prm, int dtype, const uint16_t* mask, const fd_fields* fields,
+                     void* stream);
+
+/* One getter of fingering_periodic.py:123-256 evaluated from the stored
+ * fields into `out` ((H,W)). */
+int fd_field(const fd_params* prm, int dtype, int field_id, const uint16_t* mask, const fd_fields* fields,
+             void* out, void* stream);
+
+/* ---- fused step --------------------------------------------------------- */
+
+/* `nsteps` iterations of the main loop body (fingering_periodic.py:454-479,
+ * fingering.py:558-585) as one kernel per iteration.  The state between
+ * kernels is the post-collision population pair; the kernel pulls it
+ * (stream + bounce-back + walls + Zou-He of iteration n-1), forms psi, its
+ * stencils and the macroscopic fields of iteration n, and collides.
+ *   pop_a, pop_b : two buffers of 18*H*W elements (f planes then g planes);
+ *                  the state starts in pop_a and ping-pongs; after the call
+ *                  it is in pop_a if nsteps is even, else in pop_b.
+ *   side_a, side_b: two 6*H buffers of boundary fields; the values of the
+ *                  state's iteration start in side_a and follow the same
+ *                  ping-pong.
+ * dtype: FD_F64 or FD_F32 (the storage and compute type).  W must be a
+ * multiple of 4 and H >= 3.  rows_per_warp: rows one warp marches (0 = auto). */
+int fd_fused_step(const fd_params* prm, int dtype, const uint16_t* mask, const double* inlet_ux,
+                  void* pop_a, void* pop_b, void* side_a, void* side_b, int nsteps, int rows_per_warp,
+                  void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDLBM_H */

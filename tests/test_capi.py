@@ -1,0 +1,62 @@
+"""The C-ABI library builds, loads and exports every symbol include/fdlbm.h
+declares (no GPU needed: nothing is launched)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for fn in sorted(os.listdir(os.path.join(REPO, "include"))):
+        if fn.endswith(".h"):
+            src = open(os.path.join(REPO, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(fd_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from fingering_dynamics_gb300 import build
+    path = build.build()
+    return ctypes.CDLL(path)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "fd_fused_step" in names and "fd_compute_init" in names
+    assert len(names) >= 15
+
+
+def test_every_declared_symbol_is_exported(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_abi_version_and_error_path(lib):
+    from fingering_dynamics_gb300 import _lib as L
+    assert L.lib().fd_abi_version() == 1
+    # host-side argument checks run without a GPU and report through fd_last_error
+    with pytest.raises(L.FDError) as e:
+        L.call("fd_fused_step", None, 1, None, None, None, None, None, None, 1, 0, None)
+    assert e.value.code == -1 and "NULL" in str(e.value)
+    prm = L.fd_params(10, 10, 7, 0, 0.8, 0.1, 2.0, -0.01, 0.01, 1.0, 0.0, 1.5)
+    with pytest.raises(L.FDError) as e:
+        L.call("fd_collide", ctypes.byref(prm), 1, None, None, None)
+    assert e.value.code == -1
+    prm.variant = 0
+    with pytest.raises(L.FDError) as e:
+        L.call("fd_collide", ctypes.byref(prm), 2, None, None, None)
+    assert e.value.code == -4
+
+
+def test_package_fails_loudly_without_library(monkeypatch):
+    from fingering_dynamics_gb300 import _lib as L
+    monkeypatch.setattr(L, "_handle", None)
+    monkeypatch.setattr(L, "LIB_PATH", "/nonexistent/libfdlbm.so")
+    with pytest.raises(RuntimeError, match="not built"):
+        L.lib()
