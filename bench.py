@@ -6,7 +6,7 @@ Workload (the plain FP32 fused kernel at scale): a 4096 x 2048 lattice with
 walls at the bottom and top (the walled variant, fingering.py), Zou-He plug
 inlet u_x = 0.01 and the reference's velocity-type outlet, seeded random
 circular and square blocks with radius / half-side 6..14 placed to porosity
-0.7, tau_inv = 0.55, tau_def = 1.0, interfacial tension 5e-4, contact angle
+0.7, tau_inv = 0.6, tau_def = 1.0, interfacial tension 5e-4, contact angle
 120 deg (psi_wall = cos 120 deg).  Synthetic, seeded; no dataset involved.
 
 A step is one iteration of the reference's loop body over the whole lattice
@@ -40,14 +40,19 @@ sys.path.insert(0, REPO)
 
 H_FULL, W_FULL = 2048, 4096
 SAMPLE_H, SAMPLE_W = 256, 512
-BYTES_PER_POP = {"f32": 4, "f64": 8}
+# algorithmic bytes per lattice update: every stored population read once and written once
+# (f16 / bf16 keep g_0 in FP32: 17 planes x 2 B + 1 plane x 4 B each way)
+BYTES_PER_LU = {"f64": 288, "f32": 144, "f32-exact": 144, "f16": 76, "bf16": 76}
 WORKLOAD = "walls_4096x2048_porosity0.7_blocks6-14"
+# tau_inv = 0.55 (with tau_def = 1.0) diverges within ~40 steps on this block geometry in the oracle
+# itself (the reference algorithm); 0.6 is the closest value that runs thousands of steps.
+TAU_INV = 0.6
 
 
 def workload(H, W, seed=2024):
     from fingering_dynamics_gb300 import geometry as geo
     from fingering_dynamics_gb300.params import from_relaxation_times
-    prm = from_relaxation_times(H, W, tau_inv=0.55, tau_def=1.0, sigma=5e-4, contact_angle_deg=120.0,
+    prm = from_relaxation_times(H, W, tau_inv=TAU_INV, tau_def=1.0, sigma=5e-4, contact_angle_deg=120.0,
                                 u_in=0.01, variant="walls")
     rects, circles = geo.random_blocks(H, W, 0.7, 6, 14, seed=seed, x_margin=32)
     g = geo.build_geometry(H, W, rects=rects, circles=circles, walls=True)
@@ -87,7 +92,7 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
         return self
@@ -239,12 +244,15 @@ def run_ours(args):
         barrier()
     ms_total = e0.elapsed_time(e1)
     clocks = clk.summary()
-    finite = bool(torch.isfinite(lat.pop[lat.cur]).all().item())
+    lat.exit_fused()
+    finite = bool(torch.isfinite(lat.psi).all().item())
+    lat.enter_fused()
 
     # end to end through the host-buffer API: populations in from pinned host
     # memory, one iteration, populations back out
-    host = torch.empty((18, H, W), dtype=lat.tdtype, pin_memory=True)
-    host.copy_(lat.pop[lat.cur])
+    state = lat.current_buffer()
+    host = torch.empty(state.shape, dtype=state.dtype, pin_memory=True)
+    host.copy_(state)
     e2e_steps = max(3, min(args.steps, 20))
     for _ in range(2):
         lat.upload_populations(host)
@@ -265,21 +273,21 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms_total, e2e_s = float(t[0]), float(t[1])
     if rank == 0:
-        nbytes = BYTES_PER_POP[args.dtype]
+
         ms_step = ms_total / args.steps
         cells = H * W
         mlups = world * cells * args.steps / (ms_total / 1e3) / 1e6
-        alg_bytes = 36 * nbytes * cells
+        alg_bytes = BYTES_PER_LU[args.dtype] * cells
         achieved = alg_bytes / (ms_step / 1e3) / 1e9
         peak, peak_kind = measured_peak()
-        pop_bytes = 18 * cells * nbytes
+        pop_bytes = int(state.numel() * state.element_size())
         line = {
             "metric": "MLUPS", "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
             "config": {"workload": WORKLOAD, "H": H, "W": W, "variant": "walls", "porosity": round(g.porosity, 4),
                        "blocks": len(g.rects) + len(g.circles),
-                       "tau_inv": 0.55, "tau_def": 1.0, "sigma": 5e-4, "contact_angle_deg": 120, "u_in": 0.01,
+                       "tau_inv": TAU_INV, "tau_def": 1.0, "sigma": 5e-4, "contact_angle_deg": 120, "u_in": 0.01,
                        "l2": "inputs larger than L2 (populations 2 x %d MB)" % (pop_bytes // 2 ** 20),
                        "parallelism": f"replicas{world}", "rows_per_warp": args.rows or "auto",
                        "state_finite_after_timing": finite},
@@ -303,9 +311,9 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--dtype", default="f32", choices=sorted(BYTES_PER_LU))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--rows", type=int, default=0, help="rows per warp (0 = automatic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

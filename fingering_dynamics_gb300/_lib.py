@@ -36,6 +36,10 @@ class fd_params(C.Structure):
                 ("outlet_coef", C.c_double)]
 
 
+class fd_storage(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("f_scale_log2", C.c_int32), ("g_scale_log2", C.c_int32)]
+
+
 class fd_fields(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("f", "g", "psi", "npx", "npy", "np2", "rho", "ux", "uy", "p", "mu",
                                           "mix_tau")]
@@ -43,6 +47,7 @@ class fd_fields(C.Structure):
 
 _VP, _I, _PD = C.c_void_p, C.c_int, C.c_ssize_t
 _P = C.POINTER(fd_params)
+_S = C.POINTER(fd_storage)
 _F = C.POINTER(fd_fields)
 
 # name -> argtypes (all return int status unless listed in _RET)
@@ -62,8 +67,13 @@ SIGNATURES = {
     "fd_update_macros": [_P, _I, _VP, _F, _VP],
     "fd_field": [_P, _I, _I, _VP, _F, _VP, _VP],
     "fd_fused_step": [_P, _I, _VP, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
+    "fd_packed_bytes": [_I, _I, _S],
+    "fd_pack": [_P, _I, _VP, _S, _VP, _VP],
+    "fd_unpack": [_P, _S, _VP, _I, _VP, _VP],
+    "fd_fused_step_packed": [_P, _S, _VP, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
+    "fd_device_status": [C.POINTER(C.c_uint), _I],
 }
-_RET = {"fd_last_error": C.c_char_p}
+_RET = {"fd_last_error": C.c_char_p, "fd_packed_bytes": C.c_size_t}
 
 _lock = threading.Lock()
 _handle = None

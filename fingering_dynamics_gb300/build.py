@@ -32,6 +32,8 @@ UNITS = {
     "fd_ref.cu": ["-fmad=false"],
     "fd_fused_f64.cu": ["-fmad=false"],
     "fd_fused_f32.cu": [],
+    "fd_fused_dev.cu": [],
+    "fd_fused_tma.cu": [],
 }
 
 

@@ -50,7 +50,10 @@ int fd_fused_step(const fd_params* prm, int dtype, const uint16_t* mask, const d
   FD_REQUIRE(mask && inlet_ux && pop_a && pop_b && side_a && side_b, FD_ERR_ARG, "fd_fused_step: NULL pointer");
   FD_REQUIRE(pop_a != pop_b && side_a != side_b, FD_ERR_ARG, "fd_fused_step: ping-pong buffers must differ");
   FD_REQUIRE(nsteps >= 0, FD_ERR_ARG, "fd_fused_step: negative step count");
-  const int vec = dtype == FD_F64 ? 2 : 4;
+#ifndef FD_F32_VEC
+#define FD_F32_VEC 4
+#endif
+  const int vec = dtype == FD_F64 ? 2 : FD_F32_VEC;
   FD_REQUIRE(prm->W % vec == 0 && prm->W >= 2 * vec && prm->H >= 3, FD_ERR_SHAPE,
              "fd_fused_step: W must be a multiple of %d and >= %d, H >= 3 (got %dx%d)", vec, 2 * vec, prm->H, prm->W);
   FD_REQUIRE(((uintptr_t)pop_a | (uintptr_t)pop_b | (uintptr_t)mask) % 16 == 0, FD_ERR_ARG,

@@ -1,0 +1,227 @@
+// Deviation-form physics for the FP32-compute fused kernels.
+//
+// The f populations are carried as deviations d_i = f_i - w_i from the rest
+// state rho = 1, u = 0 (optionally scaled and stored in FP16/BF16); g is
+// carried as is, with g_0 (which holds most of psi) always in FP32.  The
+// model is the reference's (fingering_periodic.py:123-264), rewritten so that
+// every quantity that is small is computed from small quantities:
+//
+//   rho = 1 + sum d_i                      j = sum d_i e_i
+//   3p - 1 = (rho - 1) + 3 psi mu          (getP, fingering_periodic.py:123-124)
+//   feq_0 - w_0 = w_0 (rho-1) - 3(1-w_0) psi mu + w_0 rho q_0
+//   feq_i - w_i = w_i ((rho-1) + 3 psi mu + rho q_i)          i >= 1
+//   geq_0 - g_0 = (sum_{i>=1} g_i) - 3(1-w_0) gamma mu + w_0 psi q_0
+//   geq_i       = w_i (3 gamma mu + psi q_i)                   i >= 1
+//   F_i = mu (1 - 1/(2 tau)) w_i [3 e_i.grad psi - 3 u.grad psi + 9 (e_i.u)(e_i.grad psi)]
+//   1/tau_mix = rho D / (6 eta1 eta2 + rho D / 2),  D = (eta1 + eta2) + (eta2 - eta1) psi
+//
+// with q_i = 3 e_i.u + 4.5 (e_i.u)^2 - 1.5 u^2, eta1 = Eta_n, eta2 = M Eta_n.
+// These are algebraically identical to the reference's expressions (the
+// mixing rule of fingering_periodic.py:201-208 is multiplied through, so the
+// reference's tau pole at D = 0 becomes 1/tau = 0).  The Zou-He rules
+// (fingering_periodic.py:268-324, fingering.py:298-390) carry over to
+// deviations because the weights they pair are equal (w1 = w3, w2 = w4,
+// w5 = w7, w6 = w8) and their weight sums are 1 or 17/18.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "fd_common.cuh"
+
+namespace fd {
+
+struct DevCoef {
+  float w[9];
+  float inv_tau_g;     // 1 / tau
+  float eta_sum;       // eta1 + eta2
+  float eta_diff;      // eta2 - eta1
+  float six_eta_prod;  // 6 eta1 eta2
+  float a, kappa;
+  float c_b0;          // 3 (1 - w0) gamma
+  float three_gamma;   // 3 gamma
+  float c_a0;          // 3 (1 - w0)
+  float psi_wall;
+  float out_coef;      // 2/3 or 1.5
+  float sf, inv_sf;    // storage scale of f deviations
+  float sg, inv_sg;    // storage scale of g_1..g_8
+};
+
+inline DevCoef make_dev_coef(const fd_params& p, int f_scale_log2, int g_scale_log2) {
+  const double w[9] = {4.0 / 9, 1.0 / 9, 1.0 / 9, 1.0 / 9, 1.0 / 9, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};
+  DevCoef c;
+  for (int i = 0; i < 9; ++i) c.w[i] = (float)w[i];
+  const double e1 = p.eta_n, e2 = p.eta_n * p.M;
+  c.inv_tau_g = (float)(1.0 / p.tau);
+  c.eta_sum = (float)(e1 + e2);
+  c.eta_diff = (float)(e2 - e1);
+  c.six_eta_prod = (float)(6.0 * e1 * e2);
+  c.a = (float)p.a;
+  c.kappa = (float)p.kappa;
+  c.c_b0 = (float)(3.0 * (1.0 - w[0]) * p.gamma);
+  c.three_gamma = (float)(3.0 * p.gamma);
+  c.c_a0 = (float)(3.0 * (1.0 - w[0]));
+  c.psi_wall = (float)p.psi_wall;
+  c.out_coef = (float)p.outlet_coef;
+  c.sf = ldexpf(1.0f, f_scale_log2);
+  c.inv_sf = ldexpf(1.0f, -f_scale_log2);
+  c.sg = ldexpf(1.0f, g_scale_log2);
+  c.inv_sg = ldexpf(1.0f, -g_scale_log2);
+  return c;
+}
+
+// ---- storage conversion -----------------------------------------------------
+template <typename S> __device__ __forceinline__ float to_f(S v);
+template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ float to_f<__half>(__half v) { return __half2float(v); }
+template <> __device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <typename S> __device__ __forceinline__ S from_f(float v);
+template <> __device__ __forceinline__ float from_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+// ---- macroscopic state of one fluid cell -------------------------------------
+struct DevMacro {
+  float drho, rho, ux, uy, psi, mu, gx, gy, inv_tau, pref;
+};
+
+__device__ __forceinline__ DevMacro dev_macros(const DevCoef& c, const float (&d)[9], float psi, float gx, float gy,
+                                               float lap) {
+  DevMacro m;
+  m.drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
+  m.rho = 1.0f + m.drho;
+  const float jx = ((d[1] - d[3]) + (d[5] - d[6])) + (d[8] - d[7]);
+  const float jy = ((d[2] - d[4]) + (d[5] - d[8])) + (d[6] - d[7]);
+  m.psi = psi;
+  m.gx = gx;
+  m.gy = gy;
+  m.mu = c.a * psi * (1.0f - psi * psi) - c.kappa * lap;  // getMu (fingering_periodic.py:141-144)
+  const float inv_rho = __frcp_rn(m.rho);
+  m.ux = fmaf(0.5f * m.mu, gx, jx) * inv_rho;             // getUx (fingering_periodic.py:126-132)
+  m.uy = fmaf(0.5f * m.mu, gy, jy) * inv_rho;
+  const float rD = m.rho * fmaf(c.eta_diff, psi, c.eta_sum);
+  m.inv_tau = rD * __frcp_rn(fmaf(0.5f, rD, c.six_eta_prod));  // 1 / getMix_tau
+  m.pref = m.mu * fmaf(-0.5f, m.inv_tau, 1.0f);              // mu (1 - 1/(2 tau))
+  return m;
+}
+
+template <int I>
+__device__ __forceinline__ void dev_collide_dir(const DevCoef& c, const DevMacro& m, float base, float ug, float usq15,
+                                                float mu3g, float& d, float& g, float S) {
+  constexpr float ex = (float)ex_of(I), ey = (float)ey_of(I);
+  const float eu = ex * m.ux + ey * m.uy;
+  const float eg = ex * m.gx + ey * m.gy;
+  const float q = fmaf(eu, fmaf(4.5f, eu, 3.0f), -usq15);
+  float deq;
+  if (I == 0) deq = fmaf(c.w[0], m.drho, fmaf(c.w[0] * m.rho, q, -c.c_a0 * m.psi * m.mu));
+  else deq = c.w[I] * fmaf(m.rho, q, base);
+  const float F = (3.0f * c.w[I] * m.pref) * fmaf(eg, fmaf(3.0f, eu, 1.0f), -ug);
+  d = fmaf(deq - d, m.inv_tau, d) + F;
+  if (I == 0) {
+    const float dg = fmaf(c.w[0] * m.psi, q, S - c.c_b0 * m.mu);  // geq_0 - g_0
+    g = fmaf(dg, c.inv_tau_g, g);
+  } else {
+    const float geq = c.w[I] * fmaf(m.psi, q, mu3g);
+    g = fmaf(geq - g, c.inv_tau_g, g);
+  }
+}
+
+__device__ __forceinline__ void dev_collide(const DevCoef& c, const DevMacro& m, float (&d)[9], float (&g)[9]) {
+  const float base = fmaf(3.0f * m.psi, m.mu, m.drho);  // 3p - 1
+  const float ug = m.ux * m.gx + m.uy * m.gy;
+  const float usq15 = 1.5f * (m.ux * m.ux + m.uy * m.uy);
+  const float mu3g = c.three_gamma * m.mu;
+  const float S = ((g[1] + g[2]) + (g[3] + g[4])) + ((g[5] + g[6]) + (g[7] + g[8]));
+  dev_collide_dir<0>(c, m, base, ug, usq15, mu3g, d[0], g[0], S);
+  dev_collide_dir<1>(c, m, base, ug, usq15, mu3g, d[1], g[1], S);
+  dev_collide_dir<2>(c, m, base, ug, usq15, mu3g, d[2], g[2], S);
+  dev_collide_dir<3>(c, m, base, ug, usq15, mu3g, d[3], g[3], S);
+  dev_collide_dir<4>(c, m, base, ug, usq15, mu3g, d[4], g[4], S);
+  dev_collide_dir<5>(c, m, base, ug, usq15, mu3g, d[5], g[5], S);
+  dev_collide_dir<6>(c, m, base, ug, usq15, mu3g, d[6], g[6], S);
+  dev_collide_dir<7>(c, m, base, ug, usq15, mu3g, d[7], g[7], S);
+  dev_collide_dir<8>(c, m, base, ug, usq15, mu3g, d[8], g[8], S);
+}
+
+// ---- Zou-He on deviations ----------------------------------------------------
+__device__ __forceinline__ float dev_inlet_D(const float (&d)[9], float gx, float mu) {
+  return ((d[0] + d[2]) + d[4]) + 2.0f * ((d[3] + d[6]) + d[7]) - 0.5f * gx * mu;
+}
+
+// rho_inlet - 1 of a row from its deviations (fingering.py:303-304)
+__device__ __forceinline__ float dev_inlet_drho(const float (&d)[9], float ux, float gx, float mu) {
+  return (dev_inlet_D(d, gx, mu) + ux) * __frcp_rn(1.0f - ux);
+}
+
+__device__ __forceinline__ void dev_zou_he_f(const DevCoef& c, int variant, int H, int W, int x, int y, float (&d)[9],
+                                             float ux, float gx, float gy, float mu, float drho_nb) {
+  const float gm6 = gx * mu * (1.0f / 6.0f), gm4 = 0.25f * gy * mu;
+  if (x == 0) {
+    if (variant == FD_VARIANT_WALLS && y == 0) {          // fingering.py:334-348
+      d[1] = d[3];
+      d[2] = d[4];
+      d[5] = d[7];
+      d[6] = 0.5f * (drho_nb - ((((d[0] + d[1]) + (d[2] + d[3])) + (d[4] + d[5])) + d[7]));
+      d[8] = d[6];
+    } else if (variant == FD_VARIANT_WALLS && y == H - 1) {  // fingering.py:350-364
+      d[1] = d[3];
+      d[4] = d[2];
+      d[8] = d[6];
+      d[5] = 0.5f * (drho_nb - ((((d[0] + d[1]) + (d[2] + d[3])) + (d[4] + d[6])) + d[8]));
+      d[7] = d[5];
+    } else {                                               // fingering_periodic.py:276-302
+      const float rho_in = (1.0f + dev_inlet_D(d, gx, mu)) * __frcp_rn(1.0f - ux);
+      const float a = ux * rho_in;
+      d[1] = d[3] + (2.0f / 3.0f) * a - gm6;
+      d[5] = d[7] - 0.5f * (d[2] - d[4]) + (1.0f / 6.0f) * a - gm6 - gm4;
+      d[8] = d[6] + 0.5f * (d[2] - d[4]) + (1.0f / 6.0f) * a - gm6 + gm4;
+    }
+  }
+  if (x == W - 1) {                                        // fingering_periodic.py:312-324
+    const float D = ((d[0] + d[2]) + d[4]) + 2.0f * ((d[1] + d[5]) + d[8]) + 0.5f * gx * mu;
+    const float a = ux * ((1.0f + D) * __frcp_rn(1.0f + ux));
+    d[3] = d[1] - c.out_coef * a + gm6;
+    d[6] = d[8] - 0.5f * (d[2] - d[4]) - (1.0f / 6.0f) * a + gm4 + gm6;
+    d[7] = d[5] + 0.5f * (d[2] - d[4]) - (1.0f / 6.0f) * a - gm4 + gm6;
+    if (variant == FD_VARIANT_WALLS) {                     // fingering.py:387-390
+      if (y == 0) d[2] = d[4];
+      if (y == H - 1) d[4] = d[2];
+    }
+  }
+}
+
+__device__ __forceinline__ void dev_zou_he_g(const DevCoef& c, int variant, int H, int W, int x, int y, float (&g)[9]) {
+  if (x == 0) {
+    if (variant == FD_VARIANT_WALLS && y == 0) {
+      g[1] = g[3];
+      g[2] = g[4];
+      g[5] = g[7];
+      g[6] = (1.0f / 36.0f) * (1.0f - (((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + g[7]))) * 18.0f;
+      g[8] = g[6];
+    } else if (variant == FD_VARIANT_WALLS && y == H - 1) {
+      g[1] = g[3];
+      g[4] = g[2];
+      g[8] = g[6];
+      g[5] = (1.0f / 36.0f) * (1.0f - (((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[6]) + g[8]))) * 18.0f;
+      g[7] = g[5];
+    } else {
+      const float psi_in = 1.0f - ((((g[0] + g[2]) + (g[3] + g[4])) + g[6]) + g[7]);
+      g[1] = (2.0f / 3.0f) * psi_in;   // w1 / (w1 + w5 + w8)
+      g[5] = (1.0f / 6.0f) * psi_in;
+      g[8] = (1.0f / 6.0f) * psi_in;
+    }
+  }
+  if (x == W - 1) {
+    const float psi_out = -1.0f - ((((g[0] + g[1]) + (g[2] + g[4])) + g[5]) + g[8]);
+    g[3] = (2.0f / 3.0f) * psi_out;
+    g[6] = (1.0f / 6.0f) * psi_out;
+    g[7] = (1.0f / 6.0f) * psi_out;
+    if (variant == FD_VARIANT_WALLS) {
+      if (y == 0) g[2] = g[4];
+      if (y == H - 1) g[4] = g[2];
+    }
+  }
+}
+
+}  // namespace fd

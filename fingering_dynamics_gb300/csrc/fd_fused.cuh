@@ -169,8 +169,12 @@ __device__ __forceinline__ void extend(const T (&p)[VEC], T (&e)[VEC + 2]) {
   e[VEC + 1] = __shfl_down_sync(0xffffffffu, p[0], 1);
 }
 
+#ifndef FD_FUSED_MINB
+#define FD_FUSED_MINB 1
+#endif
+
 template <typename T, int VEC>
-__global__ void __launch_bounds__(128) k_fused_step(const FusedArgs<T> a) {
+__global__ void __launch_bounds__(128, FD_FUSED_MINB) k_fused_step(const FusedArgs<T> a) {
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (warp >= a.nchunks * a.nstrips) return;  // warp-uniform

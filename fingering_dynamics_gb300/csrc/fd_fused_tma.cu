@@ -1,0 +1,44 @@
+// Instantiations of the shared-memory-staged fused step (fd_fused_tma.cuh)
+// and the device status word.
+#include "fd_fused_tma.cuh"
+#include "fd_host.h"
+
+#ifndef FD_TMA_NT
+#define FD_TMA_NT 128
+#endif
+#ifndef FD_TMA_NS
+#define FD_TMA_NS 5
+#endif
+
+namespace fd {
+
+int fused_tma(const fd_params& p, const fd_storage& st, const DevCoef& c, const uint16_t* mask,
+              const double* inlet_ux, void* pa, void* pb, void* sa, void* sb, int nsteps, int R, cudaStream_t s) {
+  switch (st.dtype) {
+    case FD_F16:
+      return launch_fused_tma<__half, FD_TMA_NT, FD_TMA_NS>(p, c, mask, inlet_ux, (char*)pa, (char*)pb, (float*)sa,
+                                                            (float*)sb, nsteps, R, s);
+    case FD_BF16:
+      return launch_fused_tma<__nv_bfloat16, FD_TMA_NT, FD_TMA_NS>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
+                                                                   (float*)sa, (float*)sb, nsteps, R, s);
+    default:
+      return launch_fused_tma<float, FD_TMA_NT, FD_TMA_NS>(p, c, mask, inlet_ux, (char*)pa, (char*)pb, (float*)sa,
+                                                           (float*)sb, nsteps, R, s);
+  }
+}
+
+int tma_band_width() { return FD_TMA_NT; }
+
+}  // namespace fd
+
+extern "C" int fd_device_status(unsigned* out, int clear) {
+  FD_REQUIRE(out != nullptr, FD_ERR_ARG, "fd_device_status: NULL pointer");
+  if (cudaMemcpyFromSymbol(out, fd::g_fd_device_error, sizeof(unsigned)) != cudaSuccess)
+    return fd::check_launch("fd_device_status");
+  if (clear) {
+    const unsigned zero = 0;
+    if (cudaMemcpyToSymbol(fd::g_fd_device_error, &zero, sizeof(unsigned)) != cudaSuccess)
+      return fd::check_launch("fd_device_status");
+  }
+  return FD_OK;
+}

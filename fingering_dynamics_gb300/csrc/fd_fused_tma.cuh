@@ -1,0 +1,382 @@
+// Fused step, packed deviation storage, with rows staged in shared memory by
+// bulk asynchronous copies (cp.async.bulk, completion on mbarriers).
+//
+// A CTA of NT threads owns a band of NT consecutive cells of every row of a
+// strip of R rows and marches down the strip.  Shared memory holds a ring of
+// NS row slots; a slot holds one lattice row of all 18 population planes and
+// of the mask word, for the band plus a 16-byte halo on each side.  One
+// thread issues the bulk copies of row y + NS - 2 while the CTA works on row
+// y, so global-memory latency is covered by the rows in flight instead of by
+// warps waiting on loads.
+//
+// Per row y, each thread (one cell x = x0 + t):
+//   1. pulls g of row y+1 from the ring (stream + bounce-back + Zou-He g,
+//      fingering_periodic.py:327-343, bounce_back.py, fingering_periodic.py:278-302),
+//      forms psi(y+1) (fingering_periodic.py:210-212) and writes it to a
+//      4-row psi ring (threads 0 and 1 also do the halo cells x0-1, x0+NT);
+//   2. __syncthreads: psi(y+1) complete, row y-2 no longer read;
+//   3. reads the 3x3 psi neighbourhood, pulls f of row y, applies Zou-He f,
+//      forms the macroscopic fields and collides (fingering_periodic.py:455-479),
+//      and stores the new populations to global memory.
+// Rows are loaded with wrap-around in y (the reference's np.roll); the band's
+// halo beyond the lattice's x edges is not loaded because the populations
+// streamed across x = 0 and x = W-1 are replaced by the Zou-He rules before use.
+#pragma once
+
+#include "fd_fused_dev.cuh"
+
+namespace fd {
+
+// Device-side error word: bit 0 = an mbarrier wait gave up (copy never
+// completed).  Read and cleared by fd_device_status().  This header is
+// included by exactly one translation unit.
+__device__ unsigned int g_fd_device_error = 0;
+
+constexpr unsigned kWaitLimit = 1u << 24;  // bounded spins on an mbarrier
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Wait for phase `parity` of an mbarrier, at most kWaitLimit polls.  Returns
+// false (and latches the device error word) if the phase never completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  const uint32_t a = smem_u32(bar);
+  for (unsigned it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  atomicOr(&g_fd_device_error, 1u);
+  return false;
+}
+
+// Byte layout of one ring slot for a band of NT cells.
+template <typename SF, int NT>
+struct SlotLayout {
+  static constexpr int HF = 16 / (int)sizeof(SF);     // halo elements of an SF plane
+  static constexpr int HG = 4;                        // halo elements of the FP32 g_0 plane
+  static constexpr int HM = 8;                        // halo elements of the uint16 mask row
+  static constexpr int RF = ((NT + 2 * HF) * (int)sizeof(SF) + 15) / 16 * 16;
+  static constexpr int RG = ((NT + 2 * HG) * 4 + 15) / 16 * 16;
+  static constexpr int RM = ((NT + 2 * HM) * 2 + 15) / 16 * 16;
+  static constexpr int OFF_G0 = 9 * RF;
+  static constexpr int OFF_GI = OFF_G0 + RG;
+  static constexpr int OFF_M = OFF_GI + 8 * RF;
+  static constexpr int BYTES = (OFF_M + RM + 127) / 128 * 128;
+};
+
+template <typename SF, int NT, int NS>
+struct TmaSmem {
+  static constexpr int PSI_ROW = NT + 2;
+  static constexpr int OFF_BAR = 0;
+  static constexpr int OFF_PSI = 128;
+  static constexpr int OFF_SLOT = (OFF_PSI + 4 * PSI_ROW * 4 + 127) / 128 * 128;
+  static constexpr int BYTES = OFF_SLOT + NS * SlotLayout<SF, NT>::BYTES;
+};
+
+// Issue the bulk copies of lattice row r (wrapped into [0, H)) into slot s.
+template <typename SF, int NT>
+__device__ __forceinline__ void issue_row(const DevArgs<SF>& a, char* slot, uint64_t* bar, int r, int x0) {
+  using L = SlotLayout<SF, NT>;
+  const int y = wrap(r, a.H);
+  const size_t rowoff = (size_t)y * a.W;
+  auto span = [&](int halo, int& xs, int& xe) {
+    xs = max(x0 - halo, 0);
+    xe = min(x0 + NT + halo, a.W);
+  };
+  int xs, xe, gs, ge, ms, me;
+  span(L::HF, xs, xe);
+  span(L::HG, gs, ge);
+  span(L::HM, ms, me);
+  const unsigned nf = (unsigned)((xe - xs) * sizeof(SF)), ng = (unsigned)((ge - gs) * 4), nm = (unsigned)((me - ms) * 2);
+  mbar_expect_tx(bar, 17 * nf + ng + nm);
+  const int df = (xs - (x0 - L::HF)) * (int)sizeof(SF), dg = (gs - (x0 - L::HG)) * 4, dm = (ms - (x0 - L::HM)) * 2;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) bulk_g2s(slot + i * L::RF + df, a.src_f + i * a.pstride_f + rowoff + xs, nf, bar);
+  bulk_g2s(slot + L::OFF_G0 + dg, a.src_g0 + rowoff + gs, ng, bar);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) bulk_g2s(slot + L::OFF_GI + i * L::RF + df, a.src_gi + i * a.pstride_f + rowoff + xs, nf, bar);
+  bulk_g2s(slot + L::OFF_M + dm, a.mask + rowoff + ms, nm, bar);
+}
+
+template <typename S>
+__device__ __forceinline__ float sld(const char* base, int idx, float scale) {
+  const S v = reinterpret_cast<const S*>(base)[idx];
+  if constexpr (std::is_same_v<S, float>) return v;
+  else return to_f<S>(v) * scale;
+}
+
+// Pulled populations of cell lx (band-local index, may be -1 or NT) of row
+// y: plane i comes from the slot of row y - ey_i at lx - ex_i; bounce-back
+// links replace it by the opposite plane of the same cell.  slot_of(k)
+// returns the slot of row y + k (k = -1, 0, 1).
+template <typename SF, int NT, bool IS_G>
+__device__ __forceinline__ void pull_cell(const DevCoef& c, char* const (&rows)[3], int lx, unsigned bits,
+                                          float (&v)[9]) {
+  using L = SlotLayout<SF, NT>;
+  const float s = IS_G ? c.inv_sg : c.inv_sf;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const int ey = ey_of(i), ex = ex_of(i);
+    const char* row = rows[1 - ey];  // rows[0] = y-1, rows[1] = y, rows[2] = y+1
+    if (IS_G && i == 0) v[0] = sld<float>(row + L::OFF_G0, lx + L::HG, 1.0f);
+    else if (IS_G) v[i] = sld<SF>(row + L::OFF_GI + (i - 1) * L::RF, lx - ex + L::HF, s);
+    else v[i] = sld<SF>(row + i * L::RF, lx - ex + L::HF, s);
+  }
+  if (bits) {
+#pragma unroll
+    for (int i = 1; i < 9; ++i) {
+      if (bits & (1u << (i - 1))) {
+        const int o = opp_of(i);
+        if (IS_G) v[i] = sld<SF>(rows[1] + L::OFF_GI + (o - 1) * L::RF, lx + L::HF, s);
+        else v[i] = sld<SF>(rows[1] + o * L::RF, lx + L::HF, s);
+      }
+    }
+  }
+}
+
+template <typename SF, int NT>
+__device__ __forceinline__ unsigned mask_at(const char* row, int lx) {
+  using L = SlotLayout<SF, NT>;
+  return reinterpret_cast<const uint16_t*>(row + L::OFF_M)[lx + L::HM];
+}
+
+// psi of cell x of row y (band index lx) from the ring rows y-1, y, y+1;
+// also returns its pulled g (after Zou-He) in g.
+template <typename SF, int NT>
+__device__ __forceinline__ float psi_cell(const DevArgs<SF>& a, char* const (&rows)[3], int x, int lx, int y,
+                                          float (&g)[9]) {
+  if (x < 0) return 1.0f;
+  if (x >= a.W) return -1.0f;
+  const unsigned m = mask_at<SF, NT>(rows[1], lx);
+  pull_cell<SF, NT, true>(a.c, rows, lx, m & 0xFFu, g);
+  if (x == 0 || x == a.W - 1) dev_zou_he_g(a.c, a.variant, a.H, a.W, x, y, g);
+  if (m & SOLID) return a.c.psi_wall;
+  return ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+}
+
+template <typename SF, int NT, int NS>
+__global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nbands) {
+  using L = SlotLayout<SF, NT>;
+  using M = TmaSmem<SF, NT, NS>;
+  extern __shared__ __align__(128) char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
+  float* psi_ring = reinterpret_cast<float*>(smem + M::OFF_PSI);
+  char* slots = smem + M::OFF_SLOT;
+
+  const int t = threadIdx.x;
+  const int band = blockIdx.x % nbands, strip = blockIdx.x / nbands;
+  const int x0 = band * NT;
+  const int y0 = strip * a.R, y1 = min(y0 + a.R, a.H);
+  const int x = x0 + t;
+  const bool owned = x < a.W;
+  const bool walls = a.variant == FD_VARIANT_WALLS;
+  const int first = y0 - 2, last = y1 + 1;  // rows of the ring: g of rows y0-2 .. y1+1
+
+  if (t == 0) {
+    for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int r = first; r <= min(first + NS - 1, last); ++r) {
+      const int s = (r - first) % NS;
+      issue_row<SF, NT>(a, slots + s * L::BYTES, &bars[s], r, x0);
+    }
+  }
+  bool ok = true;
+  auto slot_of = [&](int r) { return slots + ((r - first) % NS) * L::BYTES; };
+  auto wait_row = [&](int r) {
+    const int k = r - first;
+    if (ok) ok = mbar_wait(&bars[k % NS], (unsigned)((k / NS) & 1));
+  };
+  auto psi_slot = [&](int r) { return psi_ring + ((r - first) & 3) * M::PSI_ROW; };
+
+  // psi of the two rows above the first computed row's neighbourhood
+  float gC[9], gN[9];
+  for (int r = y0 - 1; r <= y0; ++r) {
+    wait_row(r - 1);
+    wait_row(r);
+    wait_row(r + 1);
+    char* const rows[3] = {slot_of(r - 1), slot_of(r), slot_of(r + 1)};
+    float* pr = psi_slot(r);
+    const bool ghost = walls && (r < 0 || r >= a.H);
+    const int yr = wrap(r, a.H);
+    float p = ghost ? a.c.psi_wall : psi_cell<SF, NT>(a, rows, x, t, yr, gN);
+    pr[t + 1] = p;
+    if (t < 2) {
+      const int hl = t == 0 ? -1 : NT;
+      float gh[9];
+      pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT>(a, rows, x0 + hl, hl, yr, gh);
+    }
+    if (r == y0) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) gC[i] = gN[i];
+    }
+  }
+
+  for (int y = y0; y < y1; ++y) {
+    // 1. psi of row y+1
+    wait_row(y + 2);
+    {
+      char* const rows[3] = {slot_of(y), slot_of(y + 1), slot_of(y + 2)};
+      const bool ghost = walls && (y + 1 >= a.H);
+      const int yr = wrap(y + 1, a.H);
+      float* pr = psi_slot(y + 1);
+      pr[t + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT>(a, rows, x, t, yr, gN);
+      if (t < 2) {
+        const int hl = t == 0 ? -1 : NT;
+        float gh[9];
+        pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT>(a, rows, x0 + hl, hl, yr, gh);
+      }
+    }
+    // rho_inlet - 1 of row 1 (bottom inlet corner) or row H-2 (top inlet
+    // corner) for the walled variant (fingering.py:341, 357).  Row H-2 pulls
+    // from row y-2, whose slot is recycled after the barrier below, so this
+    // is evaluated before it.
+    float drho_nb = 0.0f;
+    if (walls && x == 0 && (y == 0 || y == a.H - 1)) {
+      const int yn = (y == 0) ? 1 : a.H - 2;
+      char* const prow[3] = {slot_of(yn - 1), slot_of(yn), slot_of(yn + 1)};
+      float fn[9];
+      pull_cell<SF, NT, false>(a.c, prow, t, mask_at<SF, NT>(prow[1], t) & 0xFFu, fn);
+      drho_nb = dev_inlet_drho(fn, (float)a.inlet_ux[yn], a.side_in[0 * a.H + yn], a.side_in[2 * a.H + yn]);
+    }
+    // 2. psi(y+1) complete everywhere; row y-2 free for row y-2+NS
+    __syncthreads();
+    if (t == 0 && y - 2 + NS <= last) {
+      const int r = y - 2 + NS;
+      issue_row<SF, NT>(a, slot_of(r), &bars[(r - first) % NS], r, x0);
+    }
+    // 3. stencils, f pull, Zou-He, collision, store
+    if (owned) {
+      const float* pm = psi_slot(y - 1);
+      const float* pc = psi_slot(y);
+      const float* pn = psi_slot(y + 1);
+      const int j = t + 1;
+      const float C = pc[j], E = pc[j + 1], Wv = pc[j - 1], N = pn[j], S = pm[j];
+      const float NE = pn[j + 1], NW = pn[j - 1], SE = pm[j + 1], SW = pm[j - 1];
+      const float gx = (4.0f * (E - Wv) + ((NE - NW) + (SE - SW))) * (1.0f / 12.0f);
+      const float gy = (4.0f * (N - S) + ((NE + NW) - (SE + SW))) * (1.0f / 12.0f);
+      const float lap = (4.0f * ((N + S) + (E + Wv)) + ((NE + NW) + (SE + SW)) - 20.0f * C) * (1.0f / 6.0f);
+      char* const rows[3] = {slot_of(y - 1), slot_of(y), slot_of(y + 1)};
+      const unsigned m = mask_at<SF, NT>(rows[1], t);
+      float f[9];
+      pull_cell<SF, NT, false>(a.c, rows, t, m & 0xFFu, f);
+      if (x == 0 || x == a.W - 1) {
+        const int o = (x == 0) ? 0 : 3;
+        dev_zou_he_f(a.c, a.variant, a.H, a.W, x, y, f, (float)a.inlet_ux[y], a.side_in[(o + 0) * a.H + y],
+                     a.side_in[(o + 1) * a.H + y], a.side_in[(o + 2) * a.H + y], drho_nb);
+        a.side_out[(o + 0) * a.H + y] = gx;
+        a.side_out[(o + 1) * a.H + y] = gy;
+        a.side_out[(o + 2) * a.H + y] = a.c.a * C * (1.0f - C * C) - a.c.kappa * lap;
+      }
+      if (!(m & SOLID)) {
+        const DevMacro mc = dev_macros(a.c, f, C, gx, gy, lap);
+        dev_collide(a.c, mc, f, gC);
+      }
+      const size_t q = (size_t)y * a.W + x;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        if constexpr (std::is_same_v<SF, float>) a.dst_f[i * a.pstride_f + q] = f[i];
+        else a.dst_f[i * a.pstride_f + q] = from_f<SF>(f[i] * a.c.sf);
+      }
+      a.dst_g0[q] = gC[0];
+#pragma unroll
+      for (int i = 1; i < 9; ++i) {
+        if constexpr (std::is_same_v<SF, float>) a.dst_gi[(i - 1) * a.pstride_f + q] = gC[i];
+        else a.dst_gi[(i - 1) * a.pstride_f + q] = from_f<SF>(gC[i] * a.c.sg);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) gC[i] = gN[i];
+  }
+  // After a wait gave up, make sure the last copy issued into every slot has
+  // landed (bounded) before the CTA's shared memory is released.
+  if (!ok && t == 0) {
+    for (int s = 0; s < NS; ++s) {
+      const int span = last - first;
+      if (span < s) continue;
+      const int k = span - ((span - s) % NS);  // last row index (relative) filled into slot s
+      mbar_wait(&bars[s], (unsigned)((k / NS) & 1));
+    }
+  }
+}
+
+}  // namespace fd
+
+namespace fd {
+
+template <typename SF, int NT, int NS>
+int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, char* pa,
+                     char* pb, float* sa, float* sb, int nsteps, int R, cudaStream_t st) {
+  using M = TmaSmem<SF, NT, NS>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(k_fused_tma<SF, NT, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, M::BYTES) !=
+        cudaSuccess)
+      return FD_ERR_CUDA;
+    attr_set = true;
+  }
+  const PackedLayout<SF> L = packed_layout<SF>(p.H, p.W);
+  DevArgs<SF> a;
+  a.c = c;
+  a.H = p.H;
+  a.W = p.W;
+  a.variant = p.variant;
+  a.P = L.P;
+  a.pstride_f = L.pstride;
+  a.mask = mask;
+  a.inlet_ux = inlet_ux;
+  const int nbands = (p.W + NT - 1) / NT;
+  if (R <= 0) {
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tma<SF, NT, NS>, NT, M::BYTES);
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long want = 2LL * sms * (per_sm > 0 ? per_sm : 1);  // about two waves
+    long long strips = (want + nbands - 1) / nbands;
+    R = (int)((p.H + strips - 1) / strips);
+    if (R < 16) R = 16;
+    if (R > p.H) R = p.H;
+  }
+  a.R = R;
+  a.nstrips = (p.H + R - 1) / R;
+  a.nchunks = nbands;
+  const unsigned blocks = (unsigned)(nbands * a.nstrips);
+  for (int s = 0; s < nsteps; ++s) {
+    char* src = (s % 2 == 0) ? pa : pb;
+    char* dst = (s % 2 == 0) ? pb : pa;
+    a.src_f = reinterpret_cast<const SF*>(src + L.off_f);
+    a.src_g0 = reinterpret_cast<const float*>(src + L.off_g0);
+    a.src_gi = reinterpret_cast<const SF*>(src + L.off_gi);
+    a.dst_f = reinterpret_cast<SF*>(dst + L.off_f);
+    a.dst_g0 = reinterpret_cast<float*>(dst + L.off_g0);
+    a.dst_gi = reinterpret_cast<SF*>(dst + L.off_gi);
+    a.side_in = (s % 2 == 0) ? sa : sb;
+    a.side_out = (s % 2 == 0) ? sb : sa;
+    k_fused_tma<SF, NT, NS><<<blocks, NT, M::BYTES, st>>>(a, nbands);
+  }
+  return cudaGetLastError() == cudaSuccess ? FD_OK : FD_ERR_CUDA;
+}
+
+}  // namespace fd

@@ -32,7 +32,18 @@ from . import _lib as L
 from .geometry import Geometry
 from .params import LBMParams
 
-DTYPES = {"f64": (torch.float64, L.FD_F64), "f32": (torch.float32, L.FD_F32)}
+# name -> (reference-layout torch dtype, reference-layout fd dtype, packed storage or None)
+#   f64        FP64 everywhere; the fused kernel reproduces the reference bit for bit
+#   f32        FP32 reference-order kernels; fused kernel in deviation form, FP32 storage
+#   f16 / bf16 as f32, fused storage of f deviations and g_1..g_8 in FP16 / BF16 (g_0 FP32)
+#   f32-exact  FP32 with the reference's operand order in the fused kernel too
+DTYPES = {
+    "f64": (torch.float64, L.FD_F64, None),
+    "f32": (torch.float32, L.FD_F32, (L.FD_F32, 0, 0)),
+    "f16": (torch.float32, L.FD_F32, (L.FD_F16, 16, 16)),
+    "bf16": (torch.float32, L.FD_F32, (L.FD_BF16, 0, 0)),
+    "f32-exact": (torch.float32, L.FD_F32, None),
+}
 FIELD_NAMES = ("psi", "npx", "npy", "np2", "rho", "ux", "uy", "p", "mu", "mix_tau")
 
 
@@ -58,7 +69,8 @@ class Lattice:
         self.params = params
         self.geometry = geometry
         self.dtype = dtype
-        self.tdtype, self.fd_dtype = DTYPES[dtype]
+        self.tdtype, self.fd_dtype, packed = DTYPES[dtype]
+        self.storage = None if packed is None else L.fd_storage(*packed)
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise ValueError("Lattice runs on a CUDA device only")
@@ -73,6 +85,8 @@ class Lattice:
         self.side = [torch.zeros((6, H), dtype=td, device=dev) for _ in range(2)]
         self.cur = 0
         self.scur = 0
+        self.ppop = None   # packed buffers, allocated on first entry into fused mode
+        self.pcur = 0
         for n in FIELD_NAMES:
             setattr(self, n, torch.zeros((H, W), dtype=td, device=dev))
         psi0 = params.initial_psi(geometry.solid) if psi0 is None else np.asarray(psi0, np.float64)
@@ -155,6 +169,14 @@ class Lattice:
             return
         self.boundary_fields(self.side[self.scur])
         self.collide()
+        if self.storage is not None:
+            if self.ppop is None:
+                nbytes = L.lib().fd_packed_bytes(self.H, self.W, C.byref(self.storage))
+                if not nbytes:
+                    raise L.FDError(-1, "fd_packed_bytes", "invalid storage")
+                self.ppop = [torch.empty(nbytes, dtype=torch.uint8, device=self.device) for _ in range(2)]
+            L.call("fd_pack", C.byref(self.prm), self.fd_dtype, _ptr(self.pop[self.cur]), C.byref(self.storage),
+                   _ptr(self.ppop[self.pcur]), self._stream())
         self.mode = "fused"
 
     def advance(self, n: int, rows_per_warp: int = 0):
@@ -162,12 +184,21 @@ class Lattice:
         self._require("fused")
         if n <= 0:
             return
-        a, b = self.pop[self.cur], self.pop[1 - self.cur]
         sa, sb = self.side[self.scur], self.side[1 - self.scur]
-        L.call("fd_fused_step", C.byref(self.prm), self.fd_dtype, _ptr(self.mask), _ptr(self.inlet_ux), _ptr(a),
-               _ptr(b), _ptr(sa), _ptr(sb), int(n), int(rows_per_warp), self._stream())
+        if self.storage is None:
+            a, b = self.pop[self.cur], self.pop[1 - self.cur]
+            L.call("fd_fused_step", C.byref(self.prm), self.fd_dtype, _ptr(self.mask), _ptr(self.inlet_ux), _ptr(a),
+                   _ptr(b), _ptr(sa), _ptr(sb), int(n), int(rows_per_warp), self._stream())
+            if n % 2:
+                self.cur = 1 - self.cur
+        else:
+            a, b = self.ppop[self.pcur], self.ppop[1 - self.pcur]
+            L.call("fd_fused_step_packed", C.byref(self.prm), C.byref(self.storage), _ptr(self.mask),
+                   _ptr(self.inlet_ux), _ptr(a), _ptr(b), _ptr(sa), _ptr(sb), int(n), int(rows_per_warp),
+                   self._stream())
+            if n % 2:
+                self.pcur = 1 - self.pcur
         if n % 2:
-            self.cur = 1 - self.cur
             self.scur = 1 - self.scur
         self.iteration += n
 
@@ -175,6 +206,9 @@ class Lattice:
         """Finish the pending iteration; the fields become current."""
         if self.mode == "reference":
             return
+        if self.storage is not None:
+            L.call("fd_unpack", C.byref(self.prm), C.byref(self.storage), _ptr(self.ppop[self.pcur]), self.fd_dtype,
+                   _ptr(self.pop[self.cur]), self._stream())
         src, dst = self.pop[self.cur], self.pop[1 - self.cur]
         self._finish_from(src, self.side[self.scur], dst)
         self.cur = 1 - self.cur
@@ -195,14 +229,21 @@ class Lattice:
     # ------------------------------------------------------------------
     # host buffers
     # ------------------------------------------------------------------
+    def current_buffer(self) -> torch.Tensor:
+        """The device buffer that holds the state: (18, H, W) populations, or
+        the packed bytes in fused mode with packed storage."""
+        if self.mode == "fused" and self.storage is not None:
+            return self.ppop[self.pcur]
+        return self.pop[self.cur]
+
     def upload_populations(self, host: torch.Tensor):
-        """Copy (18, H, W) populations from host memory into the current
-        buffer (asynchronous when ``host`` is pinned)."""
-        self.pop[self.cur].copy_(host, non_blocking=True)
+        """Copy the state buffer from host memory (same shape and dtype as
+        :meth:`current_buffer`; asynchronous when ``host`` is pinned)."""
+        self.current_buffer().copy_(host, non_blocking=True)
 
     def download_populations(self, host: torch.Tensor):
-        """Copy the current (18, H, W) populations into host memory."""
-        host.copy_(self.pop[self.cur], non_blocking=True)
+        """Copy the state buffer into host memory."""
+        host.copy_(self.current_buffer(), non_blocking=True)
 
     # ------------------------------------------------------------------
     def state(self) -> dict:

@@ -193,6 +193,43 @@ int fd_fused_step(const fd_params* prm, int dtype, const uint16_t* mask, const d
                   void* pop_a, void* pop_b, void* side_a, void* side_b, int nsteps, int rows_per_warp,
                   void* stream);
 
+/* ---- fused step with packed (deviation) storage --------------------------- */
+
+/* Storage of the packed population buffers.  The f populations are stored as
+ * deviations (f_i - w_i) * 2^f_scale_log2 and g_1..g_8 as g_i * 2^g_scale_log2
+ * in `dtype` (FD_F32, FD_F16 or FD_BF16); g_0, which carries most of psi, is
+ * always FP32.  Arithmetic is FP32 in every case.  The layout is 18 planes of
+ * H*W elements, each starting on a 256-byte boundary: f_0..f_8, g_0, g_1..g_8.
+ * There is no counterpart in the reference (it stores float64 only). */
+typedef struct fd_storage {
+  int32_t dtype;
+  int32_t f_scale_log2;
+  int32_t g_scale_log2;
+} fd_storage;
+
+/* Bytes of one packed population buffer (0 on invalid arguments). */
+size_t fd_packed_bytes(int H, int W, const fd_storage* st);
+
+/* Reference-layout populations (18 planes of src_dtype: f then g) -> packed. */
+int fd_pack(const fd_params* prm, int src_dtype, const void* src, const fd_storage* st, void* dst, void* stream);
+
+/* Packed -> reference layout (18 planes of dst_dtype). */
+int fd_unpack(const fd_params* prm, const fd_storage* st, const void* src, int dst_dtype, void* dst, void* stream);
+
+/* fd_fused_step on packed buffers (the same loop body, fingering_periodic.py:454-479
+ * / fingering.py:558-585, computed in FP32 in deviation form).  pop_a/pop_b:
+ * fd_packed_bytes() each, 256-byte aligned; side_a/side_b: 6*H floats.
+ * W must be a multiple of 4. */
+int fd_fused_step_packed(const fd_params* prm, const fd_storage* st, const uint16_t* mask, const double* inlet_ux,
+                         void* pop_a, void* pop_b, void* side_a, void* side_b, int nsteps, int rows_per_warp,
+                         void* stream);
+
+/* Device-side status word of the library's kernels (bit 0: a bounded wait on
+ * an asynchronous copy gave up).  Copies it to *out and, if clear != 0,
+ * resets it.  Synchronous.  No counterpart in the reference (numpy raises
+ * instead, fingering_periodic.py:497). */
+int fd_device_status(unsigned* out, int clear);
+
 #ifdef __cplusplus
 }
 #endif
