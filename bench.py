@@ -223,7 +223,7 @@ def run_ours(args):
     from fingering_dynamics_gb300 import build
     from fingering_dynamics_gb300.lattice import Lattice
     build.build()
-    prm, g = workload(H_FULL, W_FULL, seed=2024 + rank)
+    prm, g = workload(args.H, args.W, seed=2024 + rank)
     lat = Lattice(prm, g, dtype=args.dtype, device=f"cuda:{local}")
     H, W = prm.H, prm.W
     lat.enter_fused()
@@ -251,22 +251,24 @@ def run_ours(args):
     # end to end through the host-buffer API: populations in from pinned host
     # memory, one iteration, populations back out
     state = lat.current_buffer()
-    host = torch.empty(state.shape, dtype=state.dtype, pin_memory=True)
-    host.copy_(state)
     e2e_steps = max(3, min(args.steps, 20))
-    for _ in range(2):
-        lat.upload_populations(host)
-        lat.advance(1, args.rows)
-        lat.download_populations(host)
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        lat.upload_populations(host)
-        lat.advance(1, args.rows)
-        lat.download_populations(host)
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = float("nan")
+    if not args.no_e2e:
+        host = torch.empty(state.shape, dtype=state.dtype, pin_memory=True)
+        host.copy_(state)
+        for _ in range(2):
+            lat.upload_populations(host)
+            lat.advance(1, args.rows)
+            lat.download_populations(host)
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            lat.upload_populations(host)
+            lat.advance(1, args.rows)
+            lat.download_populations(host)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
 
     t = torch.tensor([ms_total, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
     if world > 1:
@@ -285,7 +287,8 @@ def run_ours(args):
             "metric": "MLUPS", "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
-            "config": {"workload": WORKLOAD, "H": H, "W": W, "variant": "walls", "porosity": round(g.porosity, 4),
+            "config": {"workload": WORKLOAD if (H, W) == (H_FULL, W_FULL) else f"walls_{W}x{H}_porosity0.7_blocks6-14",
+                       "H": H, "W": W, "variant": "walls", "porosity": round(g.porosity, 4),
                        "blocks": len(g.rects) + len(g.circles),
                        "tau_inv": TAU_INV, "tau_def": 1.0, "sigma": 5e-4, "contact_angle_deg": 120, "u_in": 0.01,
                        "l2": "inputs larger than L2 (populations 2 x %d MB)" % (pop_bytes // 2 ** 20),
@@ -295,8 +298,9 @@ def run_ours(args):
                          "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                          "traffic": committed_traffic(f"fused_{args.dtype}_{W}x{H}"),
                          "algorithmic_bytes_per_launch": alg_bytes},
-            "e2e": {"value": round(world * cells * e2e_steps / e2e_s / 1e6, 1), "unit": "MLUPS",
-                    "h2d_bytes_per_step": pop_bytes, "d2h_bytes_per_step": pop_bytes},
+            "e2e": None if args.no_e2e else {
+                "value": round(world * cells * e2e_steps / e2e_s / 1e6, 1), "unit": "MLUPS",
+                "h2d_bytes_per_step": pop_bytes, "d2h_bytes_per_step": pop_bytes},
             "gpu_launches": args.steps,
             "clocks": clocks,
         }
@@ -317,6 +321,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--rows", type=int, default=0, help="rows per warp (0 = automatic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end measurement")
+    ap.add_argument("--H", type=int, default=H_FULL, help="lattice rows (default: the 4096 x 2048 workload)")
+    ap.add_argument("--W", type=int, default=W_FULL, help="lattice columns")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -106,25 +106,46 @@ __device__ __forceinline__ DevMacro dev_macros(const DevCoef& c, const float (&d
   return m;
 }
 
+// D2Q9 weights as compile-time constants (fingering_periodic.py:50-89)
+template <int I>
+__device__ __forceinline__ constexpr float wgt() {
+  return I == 0 ? 4.0f / 9.0f : (I <= 4 ? 1.0f / 9.0f : 1.0f / 36.0f);
+}
+
+// e_i . v for a compile-time direction, without multiplications by 0 or +-1
+template <int I>
+__device__ __forceinline__ float edot(float vx, float vy) {
+  constexpr int ex = ex_of(I), ey = ey_of(I);
+  if constexpr (ex == 0 && ey == 0) return 0.0f;
+  else if constexpr (ey == 0) return ex > 0 ? vx : -vx;
+  else if constexpr (ex == 0) return ey > 0 ? vy : -vy;
+  else if constexpr (ex > 0 && ey > 0) return vx + vy;
+  else if constexpr (ex < 0 && ey > 0) return vy - vx;
+  else if constexpr (ex < 0 && ey < 0) return -(vx + vy);
+  else return vx - vy;
+}
+
 template <int I>
 __device__ __forceinline__ void dev_collide_dir(const DevCoef& c, const DevMacro& m, float base, float ug, float usq15,
                                                 float mu3g, float& d, float& g, float S) {
-  constexpr float ex = (float)ex_of(I), ey = (float)ey_of(I);
-  const float eu = ex * m.ux + ey * m.uy;
-  const float eg = ex * m.gx + ey * m.gy;
-  const float q = fmaf(eu, fmaf(4.5f, eu, 3.0f), -usq15);
-  float deq;
-  if (I == 0) deq = fmaf(c.w[0], m.drho, fmaf(c.w[0] * m.rho, q, -c.c_a0 * m.psi * m.mu));
-  else deq = c.w[I] * fmaf(m.rho, q, base);
-  const float F = (3.0f * c.w[I] * m.pref) * fmaf(eg, fmaf(3.0f, eu, 1.0f), -ug);
-  d = fmaf(deq - d, m.inv_tau, d) + F;
-  if (I == 0) {
-    const float dg = fmaf(c.w[0] * m.psi, q, S - c.c_b0 * m.mu);  // geq_0 - g_0
+  const float eu = edot<I>(m.ux, m.uy);
+  const float eg = edot<I>(m.gx, m.gy);
+  constexpr float w = wgt<I>();
+  float deq, F;
+  if constexpr (I == 0) {
+    const float q = -usq15;
+    deq = fmaf(w, m.drho, fmaf(w * m.rho, q, -c.c_a0 * m.psi * m.mu));
+    F = -(3.0f * w) * m.pref * ug;
+    const float dg = fmaf(w * m.psi, q, S - c.c_b0 * m.mu);  // geq_0 - g_0
     g = fmaf(dg, c.inv_tau_g, g);
   } else {
-    const float geq = c.w[I] * fmaf(m.psi, q, mu3g);
+    const float q = fmaf(eu, fmaf(4.5f, eu, 3.0f), -usq15);
+    deq = w * fmaf(m.rho, q, base);
+    F = ((3.0f * w) * m.pref) * fmaf(eg, fmaf(3.0f, eu, 1.0f), -ug);
+    const float geq = w * fmaf(m.psi, q, mu3g);
     g = fmaf(geq - g, c.inv_tau_g, g);
   }
+  d = fmaf(deq - d, m.inv_tau, d) + F;
 }
 
 __device__ __forceinline__ void dev_collide(const DevCoef& c, const DevMacro& m, float (&d)[9], float (&g)[9]) {

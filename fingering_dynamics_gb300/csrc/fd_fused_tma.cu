@@ -12,18 +12,25 @@
 
 namespace fd {
 
+template <typename SF>
+int fused_tma_t(const fd_params& p, const fd_storage& st, const DevCoef& c, const uint16_t* mask,
+                const double* inlet_ux, void* pa, void* pb, void* sa, void* sb, int nsteps, int R, cudaStream_t s) {
+  const bool scaled = st.f_scale_log2 != 0 || st.g_scale_log2 != 0;
+  if (scaled)
+    return launch_fused_tma<SF, FD_TMA_NT, FD_TMA_NS, true>(p, c, mask, inlet_ux, (char*)pa, (char*)pb, (float*)sa,
+                                                            (float*)sb, nsteps, R, s);
+  return launch_fused_tma<SF, FD_TMA_NT, FD_TMA_NS, false>(p, c, mask, inlet_ux, (char*)pa, (char*)pb, (float*)sa,
+                                                           (float*)sb, nsteps, R, s);
+}
+
 int fused_tma(const fd_params& p, const fd_storage& st, const DevCoef& c, const uint16_t* mask,
               const double* inlet_ux, void* pa, void* pb, void* sa, void* sb, int nsteps, int R, cudaStream_t s) {
   switch (st.dtype) {
-    case FD_F16:
-      return launch_fused_tma<__half, FD_TMA_NT, FD_TMA_NS>(p, c, mask, inlet_ux, (char*)pa, (char*)pb, (float*)sa,
-                                                            (float*)sb, nsteps, R, s);
-    case FD_BF16:
-      return launch_fused_tma<__nv_bfloat16, FD_TMA_NT, FD_TMA_NS>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
-                                                                   (float*)sa, (float*)sb, nsteps, R, s);
+    case FD_F16: return fused_tma_t<__half>(p, st, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, s);
+    case FD_BF16: return fused_tma_t<__nv_bfloat16>(p, st, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, s);
     default:
-      return launch_fused_tma<float, FD_TMA_NT, FD_TMA_NS>(p, c, mask, inlet_ux, (char*)pa, (char*)pb, (float*)sa,
-                                                           (float*)sb, nsteps, R, s);
+      return launch_fused_tma<float, FD_TMA_NT, FD_TMA_NS, false>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
+                                                                  (float*)sa, (float*)sb, nsteps, R, s);
   }
 }
 

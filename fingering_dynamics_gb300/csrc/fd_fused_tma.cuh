@@ -117,70 +117,72 @@ __device__ __forceinline__ void issue_row(const DevArgs<SF>& a, char* slot, uint
   bulk_g2s(slot + L::OFF_M + dm, a.mask + rowoff + ms, nm, bar);
 }
 
-template <typename S>
-__device__ __forceinline__ float sld(const char* base, int idx, float scale) {
-  const S v = reinterpret_cast<const S*>(base)[idx];
+// Shared-memory load of element idx of a plane row at byte offset `off` from
+// the shared-memory base, converted to FP32 (times `scale` for scaled storage).
+template <typename S, bool SCALED>
+__device__ __forceinline__ float sld(const char* sm, int off, int idx, float scale) {
+  const S v = reinterpret_cast<const S*>(sm + off)[idx];
   if constexpr (std::is_same_v<S, float>) return v;
-  else return to_f<S>(v) * scale;
+  else if constexpr (SCALED) return to_f<S>(v) * scale;
+  else return to_f<S>(v);
 }
 
-// Pulled populations of cell lx (band-local index, may be -1 or NT) of row
-// y: plane i comes from the slot of row y - ey_i at lx - ex_i; bounce-back
-// links replace it by the opposite plane of the same cell.  slot_of(k)
-// returns the slot of row y + k (k = -1, 0, 1).
-template <typename SF, int NT, bool IS_G>
-__device__ __forceinline__ void pull_cell(const DevCoef& c, char* const (&rows)[3], int lx, unsigned bits,
-                                          float (&v)[9]) {
+// Pulled populations of band cell lx (may be -1 or NT) of row y.  rows[k]
+// is the byte offset of the slot of row y - 1 + k.  Plane i comes from row
+// y - ey_i at lx - ex_i; bounce-back links replace it by the opposite plane
+// of the same cell (bounce_back.py).
+template <typename SF, int NT, bool IS_G, bool SCALED>
+__device__ __forceinline__ void pull_cell(const char* sm, const DevCoef& c, const int (&rows)[3], int lx,
+                                          unsigned bits, float (&v)[9]) {
   using L = SlotLayout<SF, NT>;
   const float s = IS_G ? c.inv_sg : c.inv_sf;
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
-    const int ey = ey_of(i), ex = ex_of(i);
-    const char* row = rows[1 - ey];  // rows[0] = y-1, rows[1] = y, rows[2] = y+1
-    if (IS_G && i == 0) v[0] = sld<float>(row + L::OFF_G0, lx + L::HG, 1.0f);
-    else if (IS_G) v[i] = sld<SF>(row + L::OFF_GI + (i - 1) * L::RF, lx - ex + L::HF, s);
-    else v[i] = sld<SF>(row + i * L::RF, lx - ex + L::HF, s);
+    const int row = rows[1 - ey_of(i)];
+    if (IS_G && i == 0) v[0] = sld<float, false>(sm, row + L::OFF_G0, lx + L::HG, 1.0f);
+    else if (IS_G) v[i] = sld<SF, SCALED>(sm, row + L::OFF_GI + (i - 1) * L::RF, lx - ex_of(i) + L::HF, s);
+    else v[i] = sld<SF, SCALED>(sm, row + i * L::RF, lx - ex_of(i) + L::HF, s);
   }
   if (bits) {
 #pragma unroll
     for (int i = 1; i < 9; ++i) {
       if (bits & (1u << (i - 1))) {
         const int o = opp_of(i);
-        if (IS_G) v[i] = sld<SF>(rows[1] + L::OFF_GI + (o - 1) * L::RF, lx + L::HF, s);
-        else v[i] = sld<SF>(rows[1] + o * L::RF, lx + L::HF, s);
+        if (IS_G) v[i] = sld<SF, SCALED>(sm, rows[1] + L::OFF_GI + (o - 1) * L::RF, lx + L::HF, s);
+        else v[i] = sld<SF, SCALED>(sm, rows[1] + o * L::RF, lx + L::HF, s);
       }
     }
   }
 }
 
 template <typename SF, int NT>
-__device__ __forceinline__ unsigned mask_at(const char* row, int lx) {
+__device__ __forceinline__ unsigned mask_at(const char* sm, int row, int lx) {
   using L = SlotLayout<SF, NT>;
-  return reinterpret_cast<const uint16_t*>(row + L::OFF_M)[lx + L::HM];
+  return reinterpret_cast<const uint16_t*>(sm + row + L::OFF_M)[lx + L::HM];
 }
 
-// psi of cell x of row y (band index lx) from the ring rows y-1, y, y+1;
-// also returns its pulled g (after Zou-He) in g.
-template <typename SF, int NT>
-__device__ __forceinline__ float psi_cell(const DevArgs<SF>& a, char* const (&rows)[3], int x, int lx, int y,
-                                          float (&g)[9]) {
+// psi of cell x (band index lx) of row y from its pulled g after Zou-He
+// (fingering_periodic.py:210-212, 278-302); the pulled g is returned in g.
+template <typename SF, int NT, bool SCALED>
+__device__ __forceinline__ float psi_cell(const char* sm, const DevArgs<SF>& a, const int (&rows)[3], int x, int lx,
+                                          int y, float (&g)[9]) {
   if (x < 0) return 1.0f;
   if (x >= a.W) return -1.0f;
-  const unsigned m = mask_at<SF, NT>(rows[1], lx);
-  pull_cell<SF, NT, true>(a.c, rows, lx, m & 0xFFu, g);
+  const unsigned m = mask_at<SF, NT>(sm, rows[1], lx);
+  pull_cell<SF, NT, true, SCALED>(sm, a.c, rows, lx, m & 0xFFu, g);
   if (x == 0 || x == a.W - 1) dev_zou_he_g(a.c, a.variant, a.H, a.W, x, y, g);
   if (m & SOLID) return a.c.psi_wall;
   return ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
 }
 
-template <typename SF, int NT, int NS>
+template <typename SF, int NT, int NS, bool SCALED>
 __global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nbands) {
+  static_assert(NS == 5, "the slot rotation below keeps rows y-2 .. y+2 in five slots");
   using L = SlotLayout<SF, NT>;
   using M = TmaSmem<SF, NT, NS>;
   extern __shared__ __align__(128) char smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
   float* psi_ring = reinterpret_cast<float*>(smem + M::OFF_PSI);
-  char* slots = smem + M::OFF_SLOT;
 
   const int t = threadIdx.x;
   const int band = blockIdx.x % nbands, strip = blockIdx.x / nbands;
@@ -189,98 +191,103 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nband
   const int x = x0 + t;
   const bool owned = x < a.W;
   const bool walls = a.variant == FD_VARIANT_WALLS;
-  const int first = y0 - 2, last = y1 + 1;  // rows of the ring: g of rows y0-2 .. y1+1
+  const int first = y0 - 2, last = y1 + 1;  // ring rows: y0-2 .. y1+1
+  // halo cells of the band: the left one by thread 0, the right one by the
+  // last thread (different warps share the extra work)
+  const int hl = (t == 0) ? -1 : (t == NT - 1 ? NT : 0);
+  const bool halo = (t == 0) || (t == NT - 1);
 
   if (t == 0) {
     for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  // row first + k lives in slot k (mod 5); rows y0-2 .. y0+2 fill slots 0..4
   if (t == 0) {
-    for (int r = first; r <= min(first + NS - 1, last); ++r) {
-      const int s = (r - first) % NS;
-      issue_row<SF, NT>(a, slots + s * L::BYTES, &bars[s], r, x0);
-    }
+    for (int k = 0; k < NS && first + k <= last; ++k)
+      issue_row<SF, NT>(a, smem + M::OFF_SLOT + k * L::BYTES, &bars[k], first + k, x0);
   }
   bool ok = true;
-  auto slot_of = [&](int r) { return slots + ((r - first) % NS) * L::BYTES; };
-  auto wait_row = [&](int r) {
-    const int k = r - first;
-    if (ok) ok = mbar_wait(&bars[k % NS], (unsigned)((k / NS) & 1));
+  unsigned phase = 0;  // parity of the next fill to wait for, one bit per slot
+  auto wait_slot = [&](int s) {
+    if (ok) ok = mbar_wait(&bars[s], (phase >> s) & 1u);
+    phase ^= 1u << s;
   };
-  auto psi_slot = [&](int r) { return psi_ring + ((r - first) & 3) * M::PSI_ROW; };
+  // slots of rows y-2, y-1, y, y+1, y+2 (rotated every row) and their byte offsets
+  int si[5], so[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    si[k] = k;  // rows y0-2 .. y0+2
+    so[k] = M::OFF_SLOT + k * L::BYTES;
+  }
+  int pslot = 0;  // psi ring slot of row y0-1; rows y0-1, y0, y0+1 use pslot, +1, +2 (mod 4)
+  auto psi_row = [&](int k) { return psi_ring + ((pslot + k) & 3) * M::PSI_ROW; };
 
-  // psi of the two rows above the first computed row's neighbourhood
   float gC[9], gN[9];
-  for (int r = y0 - 1; r <= y0; ++r) {
-    wait_row(r - 1);
-    wait_row(r);
-    wait_row(r + 1);
-    char* const rows[3] = {slot_of(r - 1), slot_of(r), slot_of(r + 1)};
-    float* pr = psi_slot(r);
+  // prologue: psi of rows y0-1 and y0 (needs rows y0-2 .. y0+1)
+  wait_slot(0);
+  wait_slot(1);
+  wait_slot(2);
+  wait_slot(3);
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int r = y0 - 1 + k;
+    const int rows[3] = {so[k], so[k + 1], so[k + 2]};
+    float* pr = psi_row(k);
     const bool ghost = walls && (r < 0 || r >= a.H);
     const int yr = wrap(r, a.H);
-    float p = ghost ? a.c.psi_wall : psi_cell<SF, NT>(a, rows, x, t, yr, gN);
-    pr[t + 1] = p;
-    if (t < 2) {
-      const int hl = t == 0 ? -1 : NT;
+    pr[t + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x, t, yr, gN);
+    if (halo) {
       float gh[9];
-      pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT>(a, rows, x0 + hl, hl, yr, gh);
-    }
-    if (r == y0) {
-#pragma unroll
-      for (int i = 0; i < 9; ++i) gC[i] = gN[i];
+      pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x0 + hl, hl, yr, gh);
     }
   }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) gC[i] = gN[i];
 
   for (int y = y0; y < y1; ++y) {
-    // 1. psi of row y+1
-    wait_row(y + 2);
+    // 1. psi of row y+1 from rows y, y+1, y+2
+    wait_slot(si[4]);
     {
-      char* const rows[3] = {slot_of(y), slot_of(y + 1), slot_of(y + 2)};
+      const int rows[3] = {so[2], so[3], so[4]};
       const bool ghost = walls && (y + 1 >= a.H);
       const int yr = wrap(y + 1, a.H);
-      float* pr = psi_slot(y + 1);
-      pr[t + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT>(a, rows, x, t, yr, gN);
-      if (t < 2) {
-        const int hl = t == 0 ? -1 : NT;
+      float* pr = psi_row(2);
+      pr[t + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x, t, yr, gN);
+      if (halo) {
         float gh[9];
-        pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT>(a, rows, x0 + hl, hl, yr, gh);
+        pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x0 + hl, hl, yr, gh);
       }
     }
-    // rho_inlet - 1 of row 1 (bottom inlet corner) or row H-2 (top inlet
-    // corner) for the walled variant (fingering.py:341, 357).  Row H-2 pulls
-    // from row y-2, whose slot is recycled after the barrier below, so this
-    // is evaluated before it.
+    // rho_inlet - 1 of row 1 (bottom inlet corner, rows 0..2 = y..y+2) or of
+    // row H-2 (top inlet corner, rows H-3..H-1 = y-2..y) for the walled
+    // variant (fingering.py:341, 357); row y-2 is recycled after the barrier.
     float drho_nb = 0.0f;
     if (walls && x == 0 && (y == 0 || y == a.H - 1)) {
+      const int prow[3] = {y == 0 ? so[2] : so[0], y == 0 ? so[3] : so[1], y == 0 ? so[4] : so[2]};
       const int yn = (y == 0) ? 1 : a.H - 2;
-      char* const prow[3] = {slot_of(yn - 1), slot_of(yn), slot_of(yn + 1)};
       float fn[9];
-      pull_cell<SF, NT, false>(a.c, prow, t, mask_at<SF, NT>(prow[1], t) & 0xFFu, fn);
+      pull_cell<SF, NT, false, SCALED>(smem, a.c, prow, t, mask_at<SF, NT>(smem, prow[1], t) & 0xFFu, fn);
       drho_nb = dev_inlet_drho(fn, (float)a.inlet_ux[yn], a.side_in[0 * a.H + yn], a.side_in[2 * a.H + yn]);
     }
-    // 2. psi(y+1) complete everywhere; row y-2 free for row y-2+NS
+    // 2. psi(y+1) complete; the slot of row y-2 is free for row y+3
     __syncthreads();
-    if (t == 0 && y - 2 + NS <= last) {
-      const int r = y - 2 + NS;
-      issue_row<SF, NT>(a, slot_of(r), &bars[(r - first) % NS], r, x0);
-    }
+    if (t == 0 && y + 3 <= last) issue_row<SF, NT>(a, smem + so[0], &bars[si[0]], y + 3, x0);
     // 3. stencils, f pull, Zou-He, collision, store
     if (owned) {
-      const float* pm = psi_slot(y - 1);
-      const float* pc = psi_slot(y);
-      const float* pn = psi_slot(y + 1);
+      const float* pm = psi_row(0);
+      const float* pc = psi_row(1);
+      const float* pn = psi_row(2);
       const int j = t + 1;
       const float C = pc[j], E = pc[j + 1], Wv = pc[j - 1], N = pn[j], S = pm[j];
       const float NE = pn[j + 1], NW = pn[j - 1], SE = pm[j + 1], SW = pm[j - 1];
       const float gx = (4.0f * (E - Wv) + ((NE - NW) + (SE - SW))) * (1.0f / 12.0f);
       const float gy = (4.0f * (N - S) + ((NE + NW) - (SE + SW))) * (1.0f / 12.0f);
       const float lap = (4.0f * ((N + S) + (E + Wv)) + ((NE + NW) + (SE + SW)) - 20.0f * C) * (1.0f / 6.0f);
-      char* const rows[3] = {slot_of(y - 1), slot_of(y), slot_of(y + 1)};
-      const unsigned m = mask_at<SF, NT>(rows[1], t);
+      const int rows[3] = {so[1], so[2], so[3]};
+      const unsigned m = mask_at<SF, NT>(smem, rows[1], t);
       float f[9];
-      pull_cell<SF, NT, false>(a.c, rows, t, m & 0xFFu, f);
+      pull_cell<SF, NT, false, SCALED>(smem, a.c, rows, t, m & 0xFFu, f);
       if (x == 0 || x == a.W - 1) {
         const int o = (x == 0) ? 0 : 3;
         dev_zou_he_f(a.c, a.variant, a.H, a.W, x, y, f, (float)a.inlet_ux[y], a.side_in[(o + 0) * a.H + y],
@@ -294,20 +301,34 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nband
         dev_collide(a.c, mc, f, gC);
       }
       const size_t q = (size_t)y * a.W + x;
+      SF* pf = a.dst_f + q;
 #pragma unroll
-      for (int i = 0; i < 9; ++i) {
-        if constexpr (std::is_same_v<SF, float>) a.dst_f[i * a.pstride_f + q] = f[i];
-        else a.dst_f[i * a.pstride_f + q] = from_f<SF>(f[i] * a.c.sf);
+      for (int i = 0; i < 9; ++i, pf += a.pstride_f) {
+        if constexpr (std::is_same_v<SF, float>) *pf = f[i];
+        else if constexpr (SCALED) *pf = from_f<SF>(f[i] * a.c.sf);
+        else *pf = from_f<SF>(f[i]);
       }
       a.dst_g0[q] = gC[0];
+      SF* pg = a.dst_gi + q;
 #pragma unroll
-      for (int i = 1; i < 9; ++i) {
-        if constexpr (std::is_same_v<SF, float>) a.dst_gi[(i - 1) * a.pstride_f + q] = gC[i];
-        else a.dst_gi[(i - 1) * a.pstride_f + q] = from_f<SF>(gC[i] * a.c.sg);
+      for (int i = 1; i < 9; ++i, pg += a.pstride_f) {
+        if constexpr (std::is_same_v<SF, float>) *pg = gC[i];
+        else if constexpr (SCALED) *pg = from_f<SF>(gC[i] * a.c.sg);
+        else *pg = from_f<SF>(gC[i]);
       }
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) gC[i] = gN[i];
+    // rotate: rows y-1 .. y+3 become y-2 .. y+2 for the next row
+    const int freed = si[0], freed_off = so[0];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      si[k] = si[k + 1];
+      so[k] = so[k + 1];
+    }
+    si[4] = freed;
+    so[4] = freed_off;
+    pslot = (pslot + 1) & 3;
   }
   // After a wait gave up, make sure the last copy issued into every slot has
   // landed (bounded) before the CTA's shared memory is released.
@@ -315,7 +336,7 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nband
     for (int s = 0; s < NS; ++s) {
       const int span = last - first;
       if (span < s) continue;
-      const int k = span - ((span - s) % NS);  // last row index (relative) filled into slot s
+      const int k = span - ((span - s) % NS);  // last ring row (relative) filled into slot s
       mbar_wait(&bars[s], (unsigned)((k / NS) & 1));
     }
   }
@@ -325,13 +346,13 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nband
 
 namespace fd {
 
-template <typename SF, int NT, int NS>
+template <typename SF, int NT, int NS, bool SCALED>
 int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, char* pa,
                      char* pb, float* sa, float* sb, int nsteps, int R, cudaStream_t st) {
   using M = TmaSmem<SF, NT, NS>;
   static bool attr_set = false;
   if (!attr_set) {
-    if (cudaFuncSetAttribute(k_fused_tma<SF, NT, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, M::BYTES) !=
+    if (cudaFuncSetAttribute(k_fused_tma<SF, NT, NS, SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, M::BYTES) !=
         cudaSuccess)
       return FD_ERR_CUDA;
     attr_set = true;
@@ -349,7 +370,7 @@ int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask,
   const int nbands = (p.W + NT - 1) / NT;
   if (R <= 0) {
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tma<SF, NT, NS>, NT, M::BYTES);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tma<SF, NT, NS, SCALED>, NT, M::BYTES);
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -374,7 +395,7 @@ int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask,
     a.dst_gi = reinterpret_cast<SF*>(dst + L.off_gi);
     a.side_in = (s % 2 == 0) ? sa : sb;
     a.side_out = (s % 2 == 0) ? sb : sa;
-    k_fused_tma<SF, NT, NS><<<blocks, NT, M::BYTES, st>>>(a, nbands);
+    k_fused_tma<SF, NT, NS, SCALED><<<blocks, NT, M::BYTES, st>>>(a, nbands);
   }
   return cudaGetLastError() == cudaSuccess ? FD_OK : FD_ERR_CUDA;
 }

@@ -40,7 +40,7 @@ from .params import LBMParams
 DTYPES = {
     "f64": (torch.float64, L.FD_F64, None),
     "f32": (torch.float32, L.FD_F32, (L.FD_F32, 0, 0)),
-    "f16": (torch.float32, L.FD_F32, (L.FD_F16, 16, 16)),
+    "f16": (torch.float32, L.FD_F32, (L.FD_F16, 0, 0)),
     "bf16": (torch.float32, L.FD_F32, (L.FD_BF16, 0, 0)),
     "f32-exact": (torch.float32, L.FD_F32, None),
 }
