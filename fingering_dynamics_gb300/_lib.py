@@ -72,6 +72,7 @@ SIGNATURES = {
     "fd_unpack": [_P, _S, _VP, _I, _VP, _VP],
     "fd_fused_step_packed": [_P, _S, _VP, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
     "fd_device_status": [C.POINTER(C.c_uint), _I],
+    "fd_fused_step_packed_noalloc": [_P, _S, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
 }
 _RET = {"fd_last_error": C.c_char_p, "fd_packed_bytes": C.c_size_t}
 

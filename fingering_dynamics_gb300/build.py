@@ -34,6 +34,7 @@ UNITS = {
     "fd_fused_f32.cu": [],
     "fd_fused_dev.cu": [],
     "fd_fused_tma.cu": [],
+    "fd_noalloc.cu": [],
 }
 
 

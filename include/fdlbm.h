@@ -224,6 +224,22 @@ int fd_fused_step_packed(const fd_params* prm, const fd_storage* st, const uint1
                          void* pop_a, void* pop_b, void* side_a, void* side_b, int nsteps, int rows_per_warp,
                          void* stream);
 
+/* fd_fused_step_packed for callers that cannot allocate device memory (a
+ * host that steps inside a CUDA stream capture, or one whose memory manager
+ * owns all device memory).  The caller passes its state only: pop_a / pop_b as
+ * in fd_fused_step_packed and ONE boundary buffer `side` (6*H floats, the
+ * state's boundary values on entry and on return).  The second boundary
+ * buffer is a fixed 384 KiB array inside this library (6 x 16384 floats), held
+ * on every GPU that loads the library until the process exits; H > 16384 is
+ * rejected with FD_ERR_SCRATCH.  The first call on a device looks up that
+ * array's device address (make it before any stream capture).  All calls
+ * share the array, so calls that overlap on the GPU (other streams, other host
+ * threads) race; nothing in it needs clearing, every iteration writes all of
+ * it before it is read.  No counterpart in the reference. */
+int fd_fused_step_packed_noalloc(const fd_params* prm, const fd_storage* st, const uint16_t* mask,
+                                 const double* inlet_ux, void* pop_a, void* pop_b, void* side, int nsteps,
+                                 int rows_per_warp, void* stream);
+
 /* Device-side status word of the library's kernels (bit 0: a bounded wait on
  * an asynchronous copy gave up).  Copies it to *out and, if clear != 0,
  * resets it.  Synchronous.  No counterpart in the reference (numpy raises
