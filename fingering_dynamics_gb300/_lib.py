@@ -17,7 +17,7 @@ FD_F64, FD_F32, FD_F16, FD_BF16 = 0, 1, 2, 3
 FD_VARIANT_PERIODIC, FD_VARIANT_WALLS = 0, 1
 FD_INIT_MU, FD_INIT_UY = 1, 2
 TERMS = {"large_F": 0, "feq": 1, "geq": 2, "F": 3, "G": 4}
-FIELDS = {"rho": 0, "npx": 1, "npy": 2, "np2": 3, "mu": 4, "mu_plain": 5, "ux": 6, "uy": 7, "p": 8, "mix_tau": 9}
+FIELDS = {"rho": 0, "npx": 1, "npy": 2, "np2": 3, "mu": 4, "mu_plain": 5, "ux": 6, "uy": 7, "p": 8, "mix_tau": 9, "psi": 10}
 ERRORS = {-1: "FD_ERR_ARG", -2: "FD_ERR_SHAPE", -3: "FD_ERR_CUDA", -4: "FD_ERR_DTYPE", -5: "FD_ERR_SCRATCH"}
 
 

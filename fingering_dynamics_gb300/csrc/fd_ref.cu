@@ -317,6 +317,14 @@ __global__ void k_field(Shape s, Coef<T> c, int which, const uint16_t* __restric
     case FD_FIELD_NPY: stencil_at(F.psi, mask, s, c.psi_wall, x, y, gx, gy, lap); out[q] = gy; return;
     case FD_FIELD_NP2: stencil_at(F.psi, mask, s, c.psi_wall, x, y, gx, gy, lap); out[q] = lap; return;
     case FD_FIELD_MU_PLAIN: out[q] = chem_pot(c, F.psi[q], F.np2[q]); return;
+    case FD_FIELD_PSI:
+      if (solid) {
+        out[q] = c.psi_wall;
+      } else {
+        load_cell(F.g, s.P, q, v);
+        out[q] = sum9(v);
+      }
+      return;
     default: break;
   }
   if (solid) return;
@@ -546,7 +554,7 @@ int fd_field(const fd_params* prm, int dtype, int field_id, const uint16_t* mask
              void* stream) {
   if (int r = check_params(prm)) return r;
   if (int r = check_dtype(dtype)) return r;
-  FD_REQUIRE(field_id >= FD_FIELD_RHO && field_id <= FD_FIELD_MIX_TAU, FD_ERR_ARG, "unknown field %d", field_id);
+  FD_REQUIRE(field_id >= FD_FIELD_RHO && field_id <= FD_FIELD_PSI, FD_ERR_ARG, "unknown field %d", field_id);
   FD_REQUIRE(mask && out && fields_ok(fields), FD_ERR_ARG, "fd_field: NULL pointer");
   return dtype == FD_F64 ? launch_field<double>(*prm, field_id, mask, *fields, out, as_stream(stream))
                          : launch_field<float>(*prm, field_id, mask, *fields, out, as_stream(stream));

@@ -97,7 +97,8 @@ enum fd_field_id {
   FD_FIELD_UX = 6,       /* getUx        fingering_periodic.py:126 */
   FD_FIELD_UY = 7,       /* getUy        fingering_periodic.py:134 */
   FD_FIELD_P = 8,        /* getP         fingering_periodic.py:123 */
-  FD_FIELD_MIX_TAU = 9   /* getMix_tau   fingering_periodic.py:201 */
+  FD_FIELD_MIX_TAU = 9,  /* getMix_tau   fingering_periodic.py:201 */
+  FD_FIELD_PSI = 10      /* udpatePsi    fingering_periodic.py:210 (sum of g, psi_wall on solid) */
 };
 
 /* ---- library ------------------------------------------------------------ */
