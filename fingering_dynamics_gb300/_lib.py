@@ -40,6 +40,14 @@ class fd_storage(C.Structure):
     _fields_ = [("dtype", C.c_int32), ("f_scale_log2", C.c_int32), ("g_scale_log2", C.c_int32)]
 
 
+class fd_diag(C.Structure):
+    _fields_ = [("mass_r", C.c_double), ("mass_b", C.c_double), ("saturation", C.c_double),
+                ("invaded", C.c_int64), ("fluid", C.c_int64), ("tip_x", C.c_int32), ("breakthrough", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class fd_fields(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("f", "g", "psi", "npx", "npy", "np2", "rho", "ux", "uy", "p", "mu",
                                           "mix_tau")]
@@ -73,8 +81,10 @@ SIGNATURES = {
     "fd_fused_step_packed": [_P, _S, _VP, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
     "fd_device_status": [C.POINTER(C.c_uint), _I],
     "fd_fused_step_packed_noalloc": [_P, _S, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
+    "fd_diag_scratch_bytes": [],
+    "fd_diagnostics": [_P, _I, _S, _VP, _VP, _VP, _VP, _VP],
 }
-_RET = {"fd_last_error": C.c_char_p, "fd_packed_bytes": C.c_size_t}
+_RET = {"fd_last_error": C.c_char_p, "fd_packed_bytes": C.c_size_t, "fd_diag_scratch_bytes": C.c_size_t}
 
 _lock = threading.Lock()
 _handle = None

@@ -35,6 +35,7 @@ UNITS = {
     "fd_fused_dev.cu": [],
     "fd_fused_tma.cu": [],
     "fd_noalloc.cu": [],
+    "fd_diag.cu": [],
 }
 
 

@@ -63,7 +63,7 @@ class ComputeBase:
         walls = self._variant == L.FD_VARIANT_WALLS
         self._dtype = dtype
         self._fd = _FD_DTYPE[dtype]
-        self._dev = torch.device(device)
+        self._dev = torch.empty(0, device=device).device  # concrete index, e.g. cuda:0
         self.mask = np.asarray(mask, dtype=bool)
         if self.mask.shape != (H, W):
             raise ValueError(f"mask shape {self.mask.shape} does not match H, W = {H}, {W}")

@@ -71,9 +71,9 @@ class Lattice:
         self.dtype = dtype
         self.tdtype, self.fd_dtype, packed = DTYPES[dtype]
         self.storage = None if packed is None else L.fd_storage(*packed)
-        self.device = torch.device(device)
-        if self.device.type != "cuda":
+        if torch.device(device).type != "cuda":
             raise ValueError("Lattice runs on a CUDA device only")
+        self.device = torch.empty(0, device=device).device  # concrete index, e.g. cuda:0
         H, W = params.H, params.W
         self.H, self.W = H, W
         self.prm = make_fd_params(params)
@@ -225,6 +225,77 @@ class Lattice:
             self.exit_fused()
         else:
             self.advance(n, rows_per_warp)
+
+    # ------------------------------------------------------------------
+    # diagnostics
+    # ------------------------------------------------------------------
+    def diagnostics(self) -> dict:
+        """FP64 colour masses, saturation, finger tip and breakthrough of the
+        current state (either mode); see include/fdlbm.h ``fd_diag``."""
+        if not hasattr(self, "_diag_scratch"):
+            nbytes = L.lib().fd_diag_scratch_bytes()
+            self._diag_scratch = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            self._diag_out = torch.empty(C.sizeof(L.fd_diag), dtype=torch.uint8, device=self.device)
+        packed = self.mode == "fused" and self.storage is not None
+        buf = self.current_buffer()
+        L.call("fd_diagnostics", C.byref(self.prm), self.fd_dtype, C.byref(self.storage) if packed else None,
+               _ptr(buf), _ptr(self.mask), _ptr(self._diag_scratch), _ptr(self._diag_out), self._stream())
+        host = self._diag_out.cpu().numpy().tobytes()
+        return L.fd_diag.from_buffer_copy(host).as_dict()
+
+    # ------------------------------------------------------------------
+    # checkpoint / resume
+    # ------------------------------------------------------------------
+    def save_snapshot(self, path: str):
+        """Write the complete state to ``path`` (.npz): mode, iteration, the
+        current population buffer (reference layout or packed bytes), the
+        current boundary-value buffer and, in reference mode, the macroscopic
+        fields.  :meth:`load_snapshot` restores it exactly, so a resumed run
+        continues bit for bit."""
+        torch.cuda.current_stream(self.device).synchronize()
+        rec = {"mode": np.array(self.mode), "iteration": np.array(self.iteration), "dtype": np.array(self.dtype),
+               "H": np.array(self.H), "W": np.array(self.W), "mask_word": self.geometry.mask_word,
+               "state": self.current_buffer().cpu().numpy(), "side": self.side[self.scur].cpu().numpy()}
+        if self.mode == "reference":
+            for n in FIELD_NAMES:
+                rec[n] = getattr(self, n).cpu().numpy()
+        np.savez(path, **rec)
+
+    def load_snapshot(self, path: str):
+        """Restore a state written by :meth:`save_snapshot` into this lattice
+        (same size, dtype and geometry)."""
+        with np.load(path, allow_pickle=False) as z:
+            if (int(z["H"]), int(z["W"]), str(z["dtype"])) != (self.H, self.W, self.dtype):
+                raise ValueError("snapshot was written by a lattice of another size or dtype")
+            if not np.array_equal(z["mask_word"], self.geometry.mask_word):
+                raise ValueError("snapshot was written for another geometry")
+            mode = str(z["mode"])
+            if mode == "fused" and self.storage is not None and self.ppop is None:
+                self.mode = "reference"
+                self.enter_fused()  # allocates the packed buffers
+            self.mode = mode
+            self.iteration = int(z["iteration"])
+            self.current_buffer().copy_(torch.from_numpy(z["state"]))
+            self.side[self.scur].copy_(torch.from_numpy(z["side"]))
+            if mode == "reference":
+                for n in FIELD_NAMES:
+                    getattr(self, n).copy_(torch.from_numpy(z[n]))
+        torch.cuda.current_stream(self.device).synchronize()
+
+    def macroscopic(self) -> dict:
+        """psi, u_x, u_y (numpy, (H, W), NaN-free: 0 on solid cells for u) of
+        the current iteration; leaves the lattice in the mode it was in."""
+        fused = self.mode == "fused"
+        if fused:
+            self.exit_fused()
+        torch.cuda.current_stream(self.device).synchronize()
+        fluid = self.fluid
+        out = {"psi": self.psi.double().cpu().numpy(),
+               "ux": torch.where(fluid, self.ux, 0).double().cpu().numpy(),
+               "uy": torch.where(fluid, self.uy, 0).double().cpu().numpy()}
+        if fused:
+            self.enter_fused()
+        return out
 
     # ------------------------------------------------------------------
     # host buffers

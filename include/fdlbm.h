@@ -241,6 +241,31 @@ int fd_fused_step_packed_noalloc(const fd_params* prm, const fd_storage* st, con
                                  const double* inlet_ux, void* pop_a, void* pop_b, void* side, int nsteps,
                                  int rows_per_warp, void* stream);
 
+/* ---- diagnostics -------------------------------------------------------- */
+
+/* FP64 diagnostics of a state (no counterpart in the reference, which only
+ * plots psi; defined here as the quantities an invasion is judged by). */
+typedef struct fd_diag {
+  double mass_r;        /* sum over fluid cells of rho (1 + psi) / 2 (invading fluid) */
+  double mass_b;        /* sum over fluid cells of rho (1 - psi) / 2 (defending fluid) */
+  double saturation;    /* invaded / fluid */
+  int64_t invaded;      /* fluid cells with psi > 0 */
+  int64_t fluid;        /* fluid cells */
+  int32_t tip_x;        /* largest x of a fluid cell with psi > 0, -1 if none */
+  int32_t breakthrough; /* 1 if a fluid cell of column W-1 has psi > 0 */
+} fd_diag;
+
+/* Bytes of the scratch buffer fd_diagnostics needs (independent of the size). */
+size_t fd_diag_scratch_bytes(void);
+
+/* Diagnostics of a state held as reference-layout populations (st == NULL,
+ * dtype FD_F64 / FD_F32, 18 planes) or as a packed buffer (st != NULL).
+ * rho = sum f, psi = sum g per cell (the collision conserves both, so pre- and
+ * post-collision states agree).  `out` is a DEVICE fd_diag; accumulation is in
+ * FP64 in a fixed order, so results are reproducible. */
+int fd_diagnostics(const fd_params* prm, int dtype, const fd_storage* st, const void* pop, const uint16_t* mask,
+                   void* scratch, fd_diag* out, void* stream);
+
 /* Device-side status word of the library's kernels (bit 0: a bounded wait on
  * an asynchronous copy gave up).  Copies it to *out and, if clear != 0,
  * resets it.  Synchronous.  No counterpart in the reference (numpy raises

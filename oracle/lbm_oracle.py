@@ -427,3 +427,23 @@ def zou_he_outlet_walls(f, g, px, py, m, prm):
     _outlet_body(f, g, px, py, m, prm)
     f[2][0, -1] = f[4][0, -1]; g[2][0, -1] = g[4][0, -1]
     f[4][-1, -1] = f[2][-1, -1]; g[4][-1, -1] = g[2][-1, -1]
+
+
+def diagnostics(st: OracleState) -> dict:
+    """FP64 colour masses, saturation, finger tip and breakthrough of an
+    oracle state: the same definitions as the library's fd_diag (the reference
+    defines none of them)."""
+    m = st.mask
+    rho = st.rho
+    psi = st.psi[m]
+    xs = np.nonzero(m)[1]
+    inv = psi > 0
+    return {
+        "mass_r": float(np.sum(rho * (1.0 + psi) * 0.5)),
+        "mass_b": float(np.sum(rho * (1.0 - psi) * 0.5)),
+        "invaded": int(inv.sum()),
+        "fluid": int(m.sum()),
+        "saturation": float(inv.sum() / max(int(m.sum()), 1)),
+        "tip_x": int(xs[inv].max()) if inv.any() else -1,
+        "breakthrough": int(bool(inv[xs == st.prm.W - 1].any())),
+    }
