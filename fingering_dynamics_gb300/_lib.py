@@ -48,6 +48,11 @@ class fd_diag(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class fd_instance(C.Structure):
+    _fields_ = [("prm", fd_params), ("mask", C.c_void_p), ("inlet_ux", C.c_void_p), ("pop_a", C.c_void_p),
+                ("pop_b", C.c_void_p), ("side_a", C.c_void_p), ("side_b", C.c_void_p)]
+
+
 class fd_fields(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("f", "g", "psi", "npx", "npy", "np2", "rho", "ux", "uy", "p", "mu",
                                           "mix_tau")]
@@ -82,6 +87,12 @@ SIGNATURES = {
     "fd_device_status": [C.POINTER(C.c_uint), _I],
     "fd_fused_step_packed_noalloc": [_P, _S, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
     "fd_diag_scratch_bytes": [],
+    "fd_batch_create": [C.POINTER(fd_instance), _I, _S, _I, _I, C.POINTER(C.c_void_p)],
+    "fd_batch_configure": [_VP, _I, _I],
+    "fd_batch_step": [_VP, _I, _I, _VP],
+    "fd_batch_parity": [_VP],
+    "fd_batch_tiles": [_VP],
+    "fd_batch_destroy": [_VP],
     "fd_diagnostics": [_P, _I, _S, _VP, _VP, _VP, _VP, _VP],
 }
 _RET = {"fd_last_error": C.c_char_p, "fd_packed_bytes": C.c_size_t, "fd_diag_scratch_bytes": C.c_size_t}

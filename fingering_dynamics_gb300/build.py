@@ -36,6 +36,7 @@ UNITS = {
     "fd_fused_tma.cu": [],
     "fd_noalloc.cu": [],
     "fd_diag.cu": [],
+    "fd_batch.cu": [],
 }
 
 

@@ -175,17 +175,20 @@ __device__ __forceinline__ float psi_cell(const char* sm, const DevArgs<SF>& a, 
   return ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
 }
 
+// One strip of one band: the body shared by the single-lattice kernel and the
+// batched persistent kernel.  The mbarriers must be initialised; `phase`
+// (per-slot parity of the next fill to wait for) and `ok` carry over from
+// strip to strip.  Ends with a CTA barrier, so the ring can be refilled.
 template <typename SF, int NT, int NS, bool SCALED>
-__global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nbands) {
+__device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int strip, char* smem, unsigned& phase,
+                                          bool& ok) {
   static_assert(NS == 5, "the slot rotation below keeps rows y-2 .. y+2 in five slots");
   using L = SlotLayout<SF, NT>;
   using M = TmaSmem<SF, NT, NS>;
-  extern __shared__ __align__(128) char smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
   float* psi_ring = reinterpret_cast<float*>(smem + M::OFF_PSI);
 
   const int t = threadIdx.x;
-  const int band = blockIdx.x % nbands, strip = blockIdx.x / nbands;
   const int x0 = band * NT;
   const int y0 = strip * a.R, y1 = min(y0 + a.R, a.H);
   const int x = x0 + t;
@@ -197,18 +200,11 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nband
   const int hl = (t == 0) ? -1 : (t == NT - 1 ? NT : 0);
   const bool halo = (t == 0) || (t == NT - 1);
 
-  if (t == 0) {
-    for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
   // row first + k lives in slot k (mod 5); rows y0-2 .. y0+2 fill slots 0..4
   if (t == 0) {
     for (int k = 0; k < NS && first + k <= last; ++k)
       issue_row<SF, NT>(a, smem + M::OFF_SLOT + k * L::BYTES, &bars[k], first + k, x0);
   }
-  bool ok = true;
-  unsigned phase = 0;  // parity of the next fill to wait for, one bit per slot
   auto wait_slot = [&](int s) {
     if (ok) ok = mbar_wait(&bars[s], (phase >> s) & 1u);
     phase ^= 1u << s;
@@ -331,7 +327,7 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nband
     pslot = (pslot + 1) & 3;
   }
   // After a wait gave up, make sure the last copy issued into every slot has
-  // landed (bounded) before the CTA's shared memory is released.
+  // landed (bounded) before the ring is reused or released.
   if (!ok && t == 0) {
     for (int s = 0; s < NS; ++s) {
       const int span = last - first;
@@ -339,6 +335,51 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nband
       const int k = span - ((span - s) % NS);  // last ring row (relative) filled into slot s
       mbar_wait(&bars[s], (unsigned)((k / NS) & 1));
     }
+  }
+  ok = __syncthreads_and(ok);
+}
+
+template <typename SF, int NT, int NS>
+__device__ __forceinline__ void init_ring(char* smem) {
+  using M = TmaSmem<SF, NT, NS>;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+template <typename SF, int NT, int NS, bool SCALED>
+__global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nbands) {
+  extern __shared__ __align__(128) char smem[];
+  init_ring<SF, NT, NS>(smem);
+  unsigned phase = 0;
+  bool ok = true;
+  tma_strip<SF, NT, NS, SCALED>(a, (int)blockIdx.x % nbands, (int)blockIdx.x / nbands, smem, phase, ok);
+}
+
+// One lattice of a batch: its arguments for both ping-pong parities.
+template <typename SF>
+struct BatchInst {
+  DevArgs<SF> args[2];
+};
+
+// Persistent kernel over a tile table of (instance, band, strip) entries: CTA
+// b takes tiles b, b + gridDim.x, ...  Every instance advances one iteration.
+template <typename SF, int NT, int NS, bool SCALED>
+__global__ void __launch_bounds__(NT) k_fused_tma_batch(const BatchInst<SF>* __restrict__ inst,
+                                                        const int4* __restrict__ tiles, int ntiles, int parity) {
+  extern __shared__ __align__(128) char smem[];
+  __shared__ DevArgs<SF> sa;
+  init_ring<SF, NT, NS>(smem);
+  unsigned phase = 0;
+  bool ok = true;
+  for (int k = blockIdx.x; k < ntiles && ok; k += gridDim.x) {
+    const int4 tl = tiles[k];
+    if (threadIdx.x == 0) sa = inst[tl.x].args[parity];
+    __syncthreads();
+    tma_strip<SF, NT, NS, SCALED>(sa, tl.y, tl.z, smem, phase, ok);
   }
 }
 

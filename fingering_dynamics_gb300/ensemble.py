@@ -1,0 +1,156 @@
+"""Batched ensembles: many independent lattices advanced together.
+
+Each member is a :class:`~fingering_dynamics_gb300.lattice.Lattice` in fused
+mode with packed storage; :class:`Ensemble` hands their buffers to the C
+batch (``fd_batch_*``), which advances every member one iteration per
+persistent launch over a tile table and replays the iteration loop from a CUDA
+graph.  :meth:`Ensemble.autotune` picks the tile shape (band width and rows
+per strip) by timing the candidates on the ensemble itself.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .geometry import build_geometry, random_blocks
+from .lattice import Lattice
+from .params import LBMParams, from_relaxation_times
+
+DEFAULT_CANDIDATES = ((128, 16), (128, 32), (128, 64), (64, 32), (64, 64), (256, 16), (256, 32))
+
+
+@dataclass
+class MemberSpec:
+    """One seeded ensemble member (BASELINE's batched-ensemble generator)."""
+    H: int
+    W: int
+    porosity: float
+    viscosity_ratio: float
+    contact_angle_deg: float
+    sigma: float
+    u_in: float
+    seed: int
+
+    def build(self, tau_def: float = 1.0, variant: str = "walls"):
+        tau_inv = 0.5 + (tau_def - 0.5) / self.viscosity_ratio
+        prm = from_relaxation_times(self.H, self.W, tau_inv, tau_def, self.sigma, self.contact_angle_deg,
+                                    self.u_in, variant=variant)
+        rmax = max(3, min(14, self.H // 12))
+        rects, circles = random_blocks(self.H, self.W, self.porosity, min(6, rmax), rmax, self.seed,
+                                       x_margin=min(32, self.W // 8))
+        return prm, build_geometry(self.H, self.W, rects=rects, circles=circles, walls=variant == "walls")
+
+
+def ensemble_specs(n: int, seed: int, sizes_w=(256, 512, 1024, 2048), sizes_h=(128, 256, 512),
+                   porosity=(0.6, 0.85), ratio=(2.0, 20.0), angle=(30.0, 150.0), sigma=(1e-4, 1e-3),
+                   u_in=(0.005, 0.02)) -> list[MemberSpec]:
+    """n members drawn from a seeded generator: sizes uniform over the given
+    widths x heights, porosity uniform, viscosity ratio and interfacial
+    tension log-uniform, contact angle and inlet speed uniform."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        lr = rng.uniform(math.log(ratio[0]), math.log(ratio[1]))
+        ls = rng.uniform(math.log(sigma[0]), math.log(sigma[1]))
+        out.append(MemberSpec(H=int(rng.choice(sizes_h)), W=int(rng.choice(sizes_w)),
+                              porosity=float(rng.uniform(*porosity)), viscosity_ratio=float(math.exp(lr)),
+                              contact_angle_deg=float(rng.uniform(*angle)), sigma=float(math.exp(ls)),
+                              u_in=float(rng.uniform(*u_in)), seed=int(rng.integers(0, 2 ** 31))))
+    return out
+
+
+class Ensemble:
+    """Independent lattices advanced by one batched launch per iteration."""
+
+    def __init__(self, members, dtype: str = "f32", rows_per_strip: int = 32, band_width: int = 128,
+                 device="cuda"):
+        self.lattices = [Lattice(p, g, dtype=dtype, device=device) for p, g in members]
+        for lat in self.lattices:
+            if lat.storage is None:
+                raise ValueError("ensembles use packed storage: dtype f32, f16 or bf16")
+            lat.enter_fused()
+        self.device = self.lattices[0].device
+        self.stream = torch.cuda.Stream(device=self.device)
+        n = len(self.lattices)
+        arr = (L.fd_instance * n)()
+        for k, lat in enumerate(self.lattices):
+            arr[k] = L.fd_instance(lat.prm, lat.mask.data_ptr(), lat.inlet_ux.data_ptr(),
+                                   lat.ppop[lat.pcur].data_ptr(), lat.ppop[1 - lat.pcur].data_ptr(),
+                                   lat.side[lat.scur].data_ptr(), lat.side[1 - lat.scur].data_ptr())
+        self._inst = arr
+        self._batch = C.c_void_p()
+        L.call("fd_batch_create", arr, n, C.byref(self.lattices[0].storage), int(rows_per_strip), int(band_width),
+               C.byref(self._batch))
+        self.config = (int(band_width), int(rows_per_strip))
+        self.cells = sum(lat.H * lat.W for lat in self.lattices)
+
+    @property
+    def tiles(self) -> int:
+        return L.lib().fd_batch_tiles(self._batch)
+
+    def configure(self, band_width: int, rows_per_strip: int):
+        L.call("fd_batch_configure", self._batch, int(rows_per_strip), int(band_width))
+        self.config = (int(band_width), int(rows_per_strip))
+
+    def step(self, n: int, use_graph: bool = True):
+        """Advance every member n iterations."""
+        if n <= 0:
+            return
+        cur = torch.cuda.current_stream(self.device)
+        self.stream.wait_stream(cur)
+        L.call("fd_batch_step", self._batch, int(n), int(bool(use_graph)), C.c_void_p(self.stream.cuda_stream))
+        cur.wait_stream(self.stream)
+        if n % 2:
+            for lat in self.lattices:
+                lat.pcur ^= 1
+                lat.scur ^= 1
+        for lat in self.lattices:
+            lat.iteration += n
+
+    def time_steps(self, n: int, use_graph: bool = True) -> float:
+        """Seconds for n iterations (CUDA events on the batch stream)."""
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(self.device)
+        e0.record(self.stream)
+        L.call("fd_batch_step", self._batch, int(n), int(bool(use_graph)), C.c_void_p(self.stream.cuda_stream))
+        e1.record(self.stream)
+        torch.cuda.synchronize(self.device)
+        if n % 2:
+            for lat in self.lattices:
+                lat.pcur ^= 1
+                lat.scur ^= 1
+        for lat in self.lattices:
+            lat.iteration += n
+        return e0.elapsed_time(e1) / 1e3
+
+    def autotune(self, candidates=DEFAULT_CANDIDATES, steps: int = 20) -> dict:
+        """Time every (band width, rows per strip) candidate on this ensemble
+        and keep the fastest; returns {candidate: MLUPS}."""
+        res = {}
+        for band, rows in candidates:
+            self.configure(band, rows)
+            self.time_steps(2)
+            t = self.time_steps(steps)
+            res[(band, rows)] = self.cells * steps / t / 1e6
+        best = max(res, key=res.get)
+        self.configure(*best)
+        return res
+
+    def diagnostics(self) -> list[dict]:
+        return [lat.diagnostics() for lat in self.lattices]
+
+    def close(self):
+        if self._batch:
+            L.lib().fd_batch_destroy(self._batch)
+            self._batch = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -241,6 +241,46 @@ int fd_fused_step_packed_noalloc(const fd_params* prm, const fd_storage* st, con
                                  const double* inlet_ux, void* pop_a, void* pop_b, void* side, int nsteps,
                                  int rows_per_warp, void* stream);
 
+/* ---- batched ensemble ----------------------------------------------------- */
+
+/* One member of a batch: its parameters and its packed buffers (as for
+ * fd_fused_step_packed).  No counterpart in the reference, which runs one
+ * lattice per process. */
+typedef struct fd_instance {
+  fd_params prm;
+  const uint16_t* mask;     /* device, H*W */
+  const double* inlet_ux;   /* device, H */
+  void* pop_a;              /* device, fd_packed_bytes(): the state at parity 0 */
+  void* pop_b;
+  void* side_a;             /* device, 6*H floats: the state's boundary values at parity 0 */
+  void* side_b;
+} fd_instance;
+
+typedef struct fd_batch fd_batch;
+
+/* Build a batch over n members sharing one packed storage type (unscaled).
+ * Every iteration is one persistent launch of the staged kernel over a table
+ * of (member, band, strip) tiles: bands of band_width cells (64, 128, 256) and
+ * strips of rows_per_strip rows.  Allocates the (small) device tables. */
+int fd_batch_create(const fd_instance* inst, int n, const fd_storage* st, int rows_per_strip, int band_width,
+                    fd_batch** out);
+
+/* Change the tile shape (drops a captured graph). */
+int fd_batch_configure(fd_batch* b, int rows_per_strip, int band_width);
+
+/* Advance every member nsteps iterations on `stream`.  use_graph != 0 replays
+ * a captured two-iteration CUDA graph (needs a non-default stream; the graph
+ * is captured on first use). */
+int fd_batch_step(fd_batch* b, int nsteps, int use_graph, void* stream);
+
+/* 0 if the members' states are in pop_a / side_a, 1 if in pop_b / side_b. */
+int fd_batch_parity(const fd_batch* b);
+
+/* Number of tiles per iteration. */
+int fd_batch_tiles(const fd_batch* b);
+
+int fd_batch_destroy(fd_batch* b);
+
 /* ---- diagnostics -------------------------------------------------------- */
 
 /* FP64 diagnostics of a state (no counterpart in the reference, which only
