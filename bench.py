@@ -322,7 +322,7 @@ def run_ensemble(args):
     from fingering_dynamics_gb300 import build
     from fingering_dynamics_gb300.ensemble import Ensemble, ensemble_specs
     build.build()
-    specs = ensemble_specs(args.members, seed=2024)
+    specs = ensemble_specs(args.members, seed=2024, family=args.family)
     ens = Ensemble([s.build() for s in specs], dtype=args.dtype)
     tuned = ens.autotune(steps=10)
     for _ in range(args.warmup):
@@ -342,6 +342,7 @@ def run_ensemble(args):
             "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
             "config": {"workload": f"ensemble_{args.members}_members", "members": args.members, "cells": ens.cells,
+                       "family": args.family,
                        "tile_shape": {"band_width": ens.config[0], "rows_per_strip": ens.config[1]},
                        "autotune_mlups": {f"{b}x{r}": round(v, 1) for (b, r), v in tuned.items()},
                        "tiles_per_iteration": ens.tiles, "members_finite_after_timing": int(sum(finite)),
@@ -370,6 +371,8 @@ def main():
     ap.add_argument("--workload", default="single", choices=["single", "ensemble"],
                     help="single 4096 x 2048 lattice (default) or the batched ensemble")
     ap.add_argument("--members", type=int, default=96, help="ensemble members")
+    ap.add_argument("--family", default="stable", choices=["stable", "spec"],
+                    help="ensemble parameter family (spec: the configuration's literal ranges)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

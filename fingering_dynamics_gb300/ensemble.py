@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
-from dataclasses import dataclass
+from dataclasses import dataclass, replace
 
 import numpy as np
 import torch
@@ -19,14 +19,23 @@ import torch
 from . import _lib as L
 from .geometry import build_geometry, random_blocks
 from .lattice import Lattice
-from .params import LBMParams, from_relaxation_times
+from .params import LBMParams, from_relaxation_times, walls_reference_params
 
 DEFAULT_CANDIDATES = ((128, 16), (128, 32), (128, 64), (64, 32), (64, 64), (256, 16), (256, 32))
 
 
 @dataclass
 class MemberSpec:
-    """One seeded ensemble member (BASELINE's batched-ensemble generator)."""
+    """One seeded ensemble member.
+
+    family "spec": lattice parameters from relaxation times (tau_def = 1.0,
+    tau_inv from the viscosity ratio), interfacial tension ``sigma``, psi_wall =
+    cos(contact angle) and the reference's mobility rule.  family "stable": the
+    constants of fingering.py:16-50 with the viscosity ratio, psi_wall and inlet
+    speed of this member.  The reference model diverges within tens of steps
+    for much of the "spec" ranges on dense random obstacles (tau_inv -> 0.525,
+    mobility ~1e2-1e3 from the rule at small sigma); "stable" runs thousands.
+    """
     H: int
     W: int
     porosity: float
@@ -35,11 +44,20 @@ class MemberSpec:
     sigma: float
     u_in: float
     seed: int
+    family: str = "stable"
+    psi_wall: float = -1.0
+
+    def params(self, tau_def: float = 1.0, variant: str = "walls") -> LBMParams:
+        if self.family == "stable":
+            prm = walls_reference_params().with_size(self.H, self.W)
+            return replace(prm, M=self.viscosity_ratio, psi_wall=self.psi_wall, u0=self.u_in,
+                           inlet_ux=np.full(self.H, self.u_in))
+        tau_inv = 0.5 + (tau_def - 0.5) / self.viscosity_ratio
+        return from_relaxation_times(self.H, self.W, tau_inv, tau_def, self.sigma, self.contact_angle_deg,
+                                     self.u_in, variant=variant)
 
     def build(self, tau_def: float = 1.0, variant: str = "walls"):
-        tau_inv = 0.5 + (tau_def - 0.5) / self.viscosity_ratio
-        prm = from_relaxation_times(self.H, self.W, tau_inv, tau_def, self.sigma, self.contact_angle_deg,
-                                    self.u_in, variant=variant)
+        prm = self.params(tau_def, variant)
         rmax = max(3, min(14, self.H // 12))
         rects, circles = random_blocks(self.H, self.W, self.porosity, min(6, rmax), rmax, self.seed,
                                        x_margin=min(32, self.W // 8))
@@ -47,11 +65,15 @@ class MemberSpec:
 
 
 def ensemble_specs(n: int, seed: int, sizes_w=(256, 512, 1024, 2048), sizes_h=(128, 256, 512),
-                   porosity=(0.6, 0.85), ratio=(2.0, 20.0), angle=(30.0, 150.0), sigma=(1e-4, 1e-3),
-                   u_in=(0.005, 0.02)) -> list[MemberSpec]:
+                   porosity=(0.6, 0.85), ratio=None, angle=(30.0, 150.0), sigma=(1e-4, 1e-3),
+                   u_in=(0.005, 0.02), family: str = "stable", psi_wall=(-1.0, -0.5)) -> list[MemberSpec]:
     """n members drawn from a seeded generator: sizes uniform over the given
     widths x heights, porosity uniform, viscosity ratio and interfacial
-    tension log-uniform, contact angle and inlet speed uniform."""
+    tension log-uniform, contact angle, psi_wall and inlet speed uniform.
+    The viscosity ratio defaults to 2..20 for family "spec" (the batched
+    ensemble of the benchmark configuration) and 2..5 for "stable"."""
+    if ratio is None:
+        ratio = (2.0, 20.0) if family == "spec" else (2.0, 5.0)
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
@@ -60,7 +82,8 @@ def ensemble_specs(n: int, seed: int, sizes_w=(256, 512, 1024, 2048), sizes_h=(1
         out.append(MemberSpec(H=int(rng.choice(sizes_h)), W=int(rng.choice(sizes_w)),
                               porosity=float(rng.uniform(*porosity)), viscosity_ratio=float(math.exp(lr)),
                               contact_angle_deg=float(rng.uniform(*angle)), sigma=float(math.exp(ls)),
-                              u_in=float(rng.uniform(*u_in)), seed=int(rng.integers(0, 2 ** 31))))
+                              u_in=float(rng.uniform(*u_in)), seed=int(rng.integers(0, 2 ** 31)), family=family,
+                              psi_wall=float(rng.uniform(*psi_wall))))
     return out
 
 
