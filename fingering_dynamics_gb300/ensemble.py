@@ -92,7 +92,9 @@ class Ensemble:
 
     def __init__(self, members, dtype: str = "f32", rows_per_strip: int = 32, band_width: int = 128,
                  device="cuda"):
-        self.lattices = [Lattice(p, g, dtype=dtype, device=device) for p, g in members]
+        """members: (LBMParams, Geometry) or (LBMParams, Geometry, initial psi) tuples."""
+        self.lattices = [Lattice(m[0], m[1], dtype=dtype, device=device, psi0=m[2] if len(m) > 2 else None)
+                         for m in members]
         for lat in self.lattices:
             if lat.storage is None:
                 raise ValueError("ensembles use packed storage: dtype f32, f16 or bf16")
