@@ -67,6 +67,8 @@ def contact_angle(psi: np.ndarray, ys: float, x_center: float, min_height: float
     """Contact angle (degrees, through the psi > 0 phase) of a droplet sitting
     on the surface y = ys, from the psi = 0 crossings along each row."""
     H, W = psi.shape
+    if not np.isfinite(psi).all():
+        return float("nan")
     px, py = [], []
     xc = int(round(x_center))
     for y in range(int(math.ceil(ys + min_height)), H):
@@ -89,7 +91,7 @@ def contact_angle(psi: np.ndarray, ys: float, x_center: float, min_height: float
     return math.degrees(math.acos(c))
 
 
-def calibrate(psi_walls=(-0.9, -0.6, -0.3, 0.0, 0.3, 0.6, 0.9), steps: int = 8000, dtype: str = "f32") -> dict:
+def calibrate(psi_walls=(-0.7, -0.5, -0.3, 0.0, 0.3, 0.5, 0.7), steps: int = 8000, dtype: str = "f32") -> dict:
     """Run one droplet per psi_wall (one batched ensemble) and measure angles."""
     from .ensemble import Ensemble
     cases = [droplet_case(pw) for pw in psi_walls]

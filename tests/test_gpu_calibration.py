@@ -16,7 +16,7 @@ def test_droplet_angles_monotone_and_table_consistent():
     from fingering_dynamics_gb300 import build
     build.build()
     from fingering_dynamics_gb300.calibration import TABLE, calibrate, psi_wall_for_angle
-    res = calibrate(psi_walls=(-0.6, 0.0, 0.6), steps=6000)
+    res = calibrate(psi_walls=(-0.5, 0.0, 0.5), steps=6000)
     th = res["theta_deg"]
     assert all(math.isfinite(t) for t in th), th
     assert th[0] > th[1] > th[2], th
@@ -27,4 +27,4 @@ def test_droplet_angles_monotone_and_table_consistent():
         if ref is not None and math.isfinite(ref):
             assert abs(t - ref) < 6.0, (pw, t, ref)
     # the inverse map reproduces the table
-    assert abs(psi_wall_for_angle(table["theta_deg"][3], table) - table["psi_wall"][3]) < 1e-9
+    assert abs(psi_wall_for_angle(table["theta_deg"][3], table) - table["psi_wall"][3]) < 1e-6
