@@ -146,7 +146,7 @@ def walls_reference_params(H: int = 380, W: int = 380, psi_wall: float = -1.0, P
 def from_relaxation_times(H: int, W: int, tau_inv: float, tau_def: float, sigma: float,
                           contact_angle_deg: float, u_in: float, variant: str = "walls",
                           Pe: float = 15.0, mobility_length: float = 20.0, xi: float = 2.0,
-                          tau_g: float | None = None) -> LBMParams:
+                          tau_g: float | None = None, angle_map: str = "calibrated") -> LBMParams:
     """Parameters from lattice quantities.
 
     * ``tau_inv`` / ``tau_def``: f relaxation times of the invading (psi=+1)
@@ -158,10 +158,10 @@ def from_relaxation_times(H: int, W: int, tau_inv: float, tau_def: float, sigma:
       (fingering_periodic.py:37-39).
     * mobility: the reference's rule gamma = u0*L/((-a*Pe)*(tau-0.5))
       (fingering_periodic.py:40) with L = ``mobility_length``.
-    * contact angle: psi_wall = cos(theta).  The reference sets psi_wall
-      directly and carries no angle formula; this linear map is a stated
-      convention (theta measured through the invading fluid), not a
-      calibration.
+    * contact angle: psi_wall from the droplet calibration table
+      (fingering_dynamics_gb300.calibration; theta measured through the
+      invading fluid).  The reference sets psi_wall directly and carries no
+      angle formula.  ``angle_map="cos"`` uses psi_wall = cos(theta) instead.
     """
     tau = (1 / (3.0 - math.sqrt(3))) if tau_g is None else tau_g
     eta_n = (tau_inv - 0.5) / 3.0
@@ -169,7 +169,11 @@ def from_relaxation_times(H: int, W: int, tau_inv: float, tau_def: float, sigma:
     kappa = 0.75 * sigma * xi
     a = -2.0 * kappa / (xi ** 2)
     gamma = u_in * mobility_length / ((-a * Pe) * (tau - 0.5))
-    psi_wall = math.cos(math.radians(contact_angle_deg))
+    if angle_map == "cos":
+        psi_wall = math.cos(math.radians(contact_angle_deg))
+    else:
+        from .calibration import psi_wall_for_angle
+        psi_wall = psi_wall_for_angle(contact_angle_deg)
     if variant == "walls":
         return LBMParams(H=H, W=W, variant="walls", tau=tau, eta_n=eta_n, M=M, a=a, kappa=kappa,
                          gamma=gamma, psi_wall=psi_wall, u0=u_in, outlet_coef=1.5, inlet="plug",
