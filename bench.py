@@ -7,7 +7,7 @@ walls at the bottom and top (the walled variant, fingering.py), Zou-He plug
 inlet u_x = 0.01 and the reference's velocity-type outlet, seeded random
 circular and square blocks with radius / half-side 6..14 placed to porosity
 0.7, tau_inv = 0.6, tau_def = 1.0, interfacial tension 5e-4, contact angle
-120 deg (psi_wall = cos 120 deg).  Synthetic, seeded; no dataset involved.
+120 deg (psi_wall from the droplet calibration table).  Synthetic, seeded; no dataset involved.
 
 A step is one iteration of the reference's loop body over the whole lattice
 (one fused kernel).  `value` is lattice updates per second over all ranks
@@ -356,6 +356,33 @@ def run_ensemble(args):
     return 0
 
 
+def run_precision(args):
+    """Reduced-precision storage: error against the FP64 path on a 1024 x 256
+    instance of the same generator (max |dpsi|, colour-mass drift, saturation
+    and tip error, breakthrough iteration), one line per run."""
+    from fingering_dynamics_gb300 import build
+    from fingering_dynamics_gb300.precision import precision_study
+    build.build()
+    H, W = (256, 1024) if (args.H, args.W) == (H_FULL, W_FULL) else (args.H, args.W)
+    prm, g = workload(H, W)
+    t0 = time.perf_counter()
+    res = precision_study(prm, g, dtypes=("f32", "f16", "bf16", "f16/nearest", "bf16/nearest"), steps=args.steps,
+                          every=args.every)
+    if args.out:
+        with open(args.out, "w") as fh:
+            json.dump(res, fh)
+    per = {d: {k: v for k, v in r.items() if k != "curve"} for d, r in res["per_dtype"].items()}
+    line = {"metric": "max |psi - psi_fp64| over fluid cells, first %d iterations" % res["window"],
+            "value": per["f16"]["max_dpsi_window"], "unit": "psi", "higher_is_better": False, "n_gpus": 1,
+            "steps": args.steps, "dtype": "f16", "data": "synthetic",
+            "config": {"workload": f"walls_{W}x{H}_porosity0.7_blocks6-14", "H": H, "W": W, "every": args.every,
+                       "reference": "FP64 fused kernel (bitwise equal to the numpy oracle)"},
+            "breakthrough_f64": res["breakthrough_f64"], "per_dtype": per,
+            "wall_s": round(time.perf_counter() - t0, 1)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -368,8 +395,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end measurement")
     ap.add_argument("--H", type=int, default=H_FULL, help="lattice rows (default: the 4096 x 2048 workload)")
     ap.add_argument("--W", type=int, default=W_FULL, help="lattice columns")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble"],
-                    help="single 4096 x 2048 lattice (default) or the batched ensemble")
+    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "precision"],
+                    help="single 4096 x 2048 lattice (default), the batched ensemble, or the error study of "
+                         "reduced-precision storage against the FP64 path (1024 x 256, --steps iterations)")
+    ap.add_argument("--every", type=int, default=500, help="precision study: iterations between comparisons")
+    ap.add_argument("--out", default=None, help="precision study: write the full curves to this JSON file")
     ap.add_argument("--members", type=int, default=96, help="ensemble members")
     ap.add_argument("--family", default="stable", choices=["stable", "spec"],
                     help="ensemble parameter family (spec: the configuration's literal ranges)")
@@ -380,6 +410,8 @@ def main():
         return run_reference(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
+    if args.workload == "precision":
+        return run_precision(args)
     return run_ours(args)
 
 

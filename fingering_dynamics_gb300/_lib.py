@@ -16,6 +16,8 @@ FD_OK = 0
 FD_F64, FD_F32, FD_F16, FD_BF16 = 0, 1, 2, 3
 FD_VARIANT_PERIODIC, FD_VARIANT_WALLS = 0, 1
 FD_INIT_MU, FD_INIT_UY = 1, 2
+FD_ROUND_NEAREST, FD_ROUND_STOCHASTIC = 0, 1
+ROUNDING = {"nearest": FD_ROUND_NEAREST, "stochastic": FD_ROUND_STOCHASTIC}
 TERMS = {"large_F": 0, "feq": 1, "geq": 2, "F": 3, "G": 4}
 FIELDS = {"rho": 0, "npx": 1, "npy": 2, "np2": 3, "mu": 4, "mu_plain": 5, "ux": 6, "uy": 7, "p": 8, "mix_tau": 9, "psi": 10}
 ERRORS = {-1: "FD_ERR_ARG", -2: "FD_ERR_SHAPE", -3: "FD_ERR_CUDA", -4: "FD_ERR_DTYPE", -5: "FD_ERR_SCRATCH"}
@@ -37,7 +39,8 @@ class fd_params(C.Structure):
 
 
 class fd_storage(C.Structure):
-    _fields_ = [("dtype", C.c_int32), ("f_scale_log2", C.c_int32), ("g_scale_log2", C.c_int32)]
+    _fields_ = [("dtype", C.c_int32), ("f_scale_log2", C.c_int32), ("g_scale_log2", C.c_int32),
+                ("rounding", C.c_int32), ("seed", C.c_uint32)]
 
 
 class fd_diag(C.Structure):
@@ -50,7 +53,7 @@ class fd_diag(C.Structure):
 
 class fd_instance(C.Structure):
     _fields_ = [("prm", fd_params), ("mask", C.c_void_p), ("inlet_ux", C.c_void_p), ("pop_a", C.c_void_p),
-                ("pop_b", C.c_void_p), ("side_a", C.c_void_p), ("side_b", C.c_void_p)]
+                ("pop_b", C.c_void_p), ("side_a", C.c_void_p), ("side_b", C.c_void_p), ("seed", C.c_uint32)]
 
 
 class fd_fields(C.Structure):

@@ -21,6 +21,7 @@ struct fd_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t graph_stream = nullptr;
+  unsigned* d_steps = nullptr;  // two-slot step counter for stochastic rounding (k_fused_tma_batch)
 };
 
 namespace fd {
@@ -54,13 +55,14 @@ DevArgs<SF> instance_args(const fd_instance& in, const fd_storage& st, int rows,
   a.dst_gi = reinterpret_cast<SF*>(dst + L.off_gi);
   a.side_in = (const float*)(swap ? in.side_b : in.side_a);
   a.side_out = (float*)(swap ? in.side_a : in.side_b);
+  a.seed = in.seed;  // hashed with the batch step counter in the kernel
   return a;
 }
 
-template <typename SF, int NT>
+template <typename SF, int NT, bool STOCH>
 int prepare(fd_batch* b) {
   using M = TmaSmem<SF, NT, kNS>;
-  auto kern = k_fused_tma_batch<SF, NT, kNS, false>;
+  auto kern = k_fused_tma_batch<SF, NT, kNS, false, STOCH>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, M::BYTES) != cudaSuccess)
     return check_launch("fd_batch: shared-memory attribute");
   std::vector<BatchInst<SF>> hi(b->n);
@@ -93,44 +95,50 @@ int prepare(fd_batch* b) {
   return FD_OK;
 }
 
-template <typename SF, int NT>
+template <typename SF, int NT, bool STOCH>
 void launch_one(const fd_batch* b, int parity, cudaStream_t st) {
   using M = TmaSmem<SF, NT, kNS>;
-  k_fused_tma_batch<SF, NT, kNS, false><<<b->grid, NT, M::BYTES, st>>>(
-      (const BatchInst<SF>*)b->d_inst, b->d_tiles, b->ntiles, parity);
+  k_fused_tma_batch<SF, NT, kNS, false, STOCH><<<b->grid, NT, M::BYTES, st>>>(
+      (const BatchInst<SF>*)b->d_inst, b->d_tiles, b->ntiles, parity, b->d_steps);
 }
 
-template <typename SF>
+template <typename SF, bool STOCH>
 int prepare_t(fd_batch* b) {
   switch (b->band) {
-    case 64: return prepare<SF, 64>(b);
-    case 256: return prepare<SF, 256>(b);
-    default: return prepare<SF, 128>(b);
+    case 64: return prepare<SF, 64, STOCH>(b);
+    case 256: return prepare<SF, 256, STOCH>(b);
+    default: return prepare<SF, 128, STOCH>(b);
   }
 }
 
-template <typename SF>
+template <typename SF, bool STOCH>
 void launch_t(const fd_batch* b, int parity, cudaStream_t st) {
   switch (b->band) {
-    case 64: launch_one<SF, 64>(b, parity, st); break;
-    case 256: launch_one<SF, 256>(b, parity, st); break;
-    default: launch_one<SF, 128>(b, parity, st); break;
+    case 64: launch_one<SF, 64, STOCH>(b, parity, st); break;
+    case 256: launch_one<SF, 256, STOCH>(b, parity, st); break;
+    default: launch_one<SF, 128, STOCH>(b, parity, st); break;
   }
 }
 
+bool stochastic(const fd_batch* b) { return b->st.dtype != FD_F32 && b->st.rounding == FD_ROUND_STOCHASTIC; }
+
 int prepare_any(fd_batch* b) {
+  const bool sr = stochastic(b);
   switch (b->st.dtype) {
-    case FD_F16: return prepare_t<__half>(b);
-    case FD_BF16: return prepare_t<__nv_bfloat16>(b);
-    default: return prepare_t<float>(b);
+    case FD_F16: return sr ? prepare_t<__half, true>(b) : prepare_t<__half, false>(b);
+    case FD_BF16: return sr ? prepare_t<__nv_bfloat16, true>(b) : prepare_t<__nv_bfloat16, false>(b);
+    default: return prepare_t<float, false>(b);
   }
 }
 
 void launch_any(const fd_batch* b, int parity, cudaStream_t st) {
+  const bool sr = stochastic(b);
   switch (b->st.dtype) {
-    case FD_F16: launch_t<__half>(b, parity, st); break;
-    case FD_BF16: launch_t<__nv_bfloat16>(b, parity, st); break;
-    default: launch_t<float>(b, parity, st); break;
+    case FD_F16: sr ? launch_t<__half, true>(b, parity, st) : launch_t<__half, false>(b, parity, st); break;
+    case FD_BF16:
+      sr ? launch_t<__nv_bfloat16, true>(b, parity, st) : launch_t<__nv_bfloat16, false>(b, parity, st);
+      break;
+    default: launch_t<float, false>(b, parity, st); break;
   }
 }
 
@@ -156,6 +164,8 @@ int fd_batch_create(const fd_instance* inst, int n, const fd_storage* st, int ro
              "fd_batch_create: storage dtype %d", st->dtype);
   FD_REQUIRE(st->f_scale_log2 == 0 && st->g_scale_log2 == 0, FD_ERR_ARG,
              "fd_batch_create: scaled storage is not supported by the batched kernel");
+  FD_REQUIRE(st->rounding == FD_ROUND_NEAREST || st->rounding == FD_ROUND_STOCHASTIC, FD_ERR_ARG,
+             "fd_batch_create: storage rounding %d", st->rounding);
   FD_REQUIRE(band_width == 64 || band_width == 128 || band_width == 256, FD_ERR_ARG,
              "fd_batch_create: band width must be 64, 128 or 256");
   FD_REQUIRE(rows_per_strip >= 1, FD_ERR_ARG, "fd_batch_create: rows per strip must be positive");
@@ -175,6 +185,12 @@ int fd_batch_create(const fd_instance* inst, int n, const fd_storage* st, int ro
   b->band = band_width;
   b->rows = rows_per_strip;
   b->inst.assign(inst, inst + n);
+  if (cudaMalloc(&b->d_steps, 2 * sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(b->d_steps, 0, 2 * sizeof(unsigned)) != cudaSuccess) {
+    const int r = check_launch("fd_batch_create: step counter");
+    fd_batch_destroy(b);
+    return r;
+  }
   if (int r = prepare_any(b)) {
     fd_batch_destroy(b);
     return r;
@@ -234,6 +250,7 @@ int fd_batch_destroy(fd_batch* b) {
   drop_graph(b);
   cudaFree(b->d_inst);
   cudaFree(b->d_tiles);
+  cudaFree(b->d_steps);
   delete b;
   return FD_OK;
 }

@@ -81,6 +81,36 @@ template <> __device__ __forceinline__ float from_f<float>(float v) { return v; 
 template <> __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
 template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
 
+// ---- stochastic rounding ----------------------------------------------------
+// Counter-based randomness: a 32-bit integer hash (the "lowbias32" xorshift-
+// multiply construction, constants from its published parameter search) of
+// the cell index mixed with the step's seed, then a 32-bit linear congruential
+// sequence (Numerical Recipes' constants) for the successive stores of a
+// cell; only the high bits of each value are used.
+__host__ __device__ __forceinline__ uint32_t sr_hash(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+__device__ __forceinline__ uint32_t sr_next(uint32_t s) { return s * 1664525u + 1013904223u; }
+
+// FP32 -> storage type, rounding the magnitude up with probability equal to
+// the discarded fraction: add uniform random bits below the last kept bit of
+// the FP32 pattern, then truncate.  (Below the FP16 normal range, 6.1e-5, more
+// bits are discarded than dithered: there the rounding leans towards zero by
+// at most one FP16 subnormal step, 6e-8.)
+template <typename S> __device__ __forceinline__ S from_f_sr(float v, uint32_t r);
+template <> __device__ __forceinline__ float from_f_sr<float>(float v, uint32_t) { return v; }
+template <> __device__ __forceinline__ __half from_f_sr<__half>(float v, uint32_t r) {
+  return __float2half_rz(__uint_as_float(__float_as_uint(v) + (r >> 19)));
+}
+template <> __device__ __forceinline__ __nv_bfloat16 from_f_sr<__nv_bfloat16>(float v, uint32_t r) {
+  return __float2bfloat16_rz(__uint_as_float(__float_as_uint(v) + (r >> 16)));
+}
+
 // ---- macroscopic state of one fluid cell -------------------------------------
 struct DevMacro {
   float drho, rho, ux, uy, psi, mu, gx, gy, inv_tau, pref;
@@ -125,44 +155,75 @@ __device__ __forceinline__ float edot(float vx, float vy) {
   else return vx - vy;
 }
 
+// Relaxation of one weight class (w = 1/9: axis directions, w = 1/36:
+// diagonals) with the relaxation rates folded in:
+//   yr = w rho / tau        xr = yr / 2          xb = w (3p - 1) / tau
+//   P  = 3 w mu (1 - 1/(2 tau))                  (forcing prefactor)
+//   gt = w psi / tau_g      gs = gt / 2          gc = 3 w gamma mu / tau_g
+struct DevClass {
+  float yr, xr, xb, P, gt, gs, gc;
+};
+
+// One pair of opposite directions (I, opp I).  With t = 3 e.u and
+// s2 = t^2 - 3 u^2, q_(+-) = +-t + s2/2, so
+//   (1/tau) (feq_(+-) - w) = xr s2 + xb +- yr t
+//   F_(+-) = P (eg t - u.grad psi) +- P eg            (eg = e.grad psi)
+//   (1/tau_g) geq_(+-) = gs s2 + gc +- gt t
+// and each population relaxes as d' = (1 - 1/tau) d + [...].
 template <int I>
-__device__ __forceinline__ void dev_collide_dir(const DevCoef& c, const DevMacro& m, float base, float ug, float usq15,
-                                                float mu3g, float& d, float& g, float S) {
-  const float eu = edot<I>(m.ux, m.uy);
+__device__ __forceinline__ void dev_collide_pair(const DevMacro& m, const DevClass& k, float usq3, float ug, float omt,
+                                                 float omg, float& dp, float& dm, float& gp, float& gm) {
+  const float t = 3.0f * edot<I>(m.ux, m.uy);
   const float eg = edot<I>(m.gx, m.gy);
-  constexpr float w = wgt<I>();
-  float deq, F;
-  if constexpr (I == 0) {
-    const float q = -usq15;
-    deq = fmaf(w, m.drho, fmaf(w * m.rho, q, -c.c_a0 * m.psi * m.mu));
-    F = -(3.0f * w) * m.pref * ug;
-    const float dg = fmaf(w * m.psi, q, S - c.c_b0 * m.mu);  // geq_0 - g_0
-    g = fmaf(dg, c.inv_tau_g, g);
-  } else {
-    const float q = fmaf(eu, fmaf(4.5f, eu, 3.0f), -usq15);
-    deq = w * fmaf(m.rho, q, base);
-    F = ((3.0f * w) * m.pref) * fmaf(eg, fmaf(3.0f, eu, 1.0f), -ug);
-    const float geq = w * fmaf(m.psi, q, mu3g);
-    g = fmaf(geq - g, c.inv_tau_g, g);
-  }
-  d = fmaf(deq - d, m.inv_tau, d) + F;
+  const float s2 = fmaf(t, t, -usq3);
+  const float B = fmaf(eg, t, -ug);
+  const float Z = fmaf(k.xr, s2, fmaf(k.P, B, k.xb));
+  const float V = fmaf(k.yr, t, k.P * eg);
+  dp = fmaf(omt, dp, Z + V);
+  dm = fmaf(omt, dm, Z - V);
+  const float G = fmaf(k.gs, s2, k.gc);
+  const float Gt = k.gt * t;
+  gp = fmaf(omg, gp, G + Gt);
+  gm = fmaf(omg, gm, G - Gt);
 }
 
 __device__ __forceinline__ void dev_collide(const DevCoef& c, const DevMacro& m, float (&d)[9], float (&g)[9]) {
   const float base = fmaf(3.0f * m.psi, m.mu, m.drho);  // 3p - 1
   const float ug = m.ux * m.gx + m.uy * m.gy;
-  const float usq15 = 1.5f * (m.ux * m.ux + m.uy * m.uy);
-  const float mu3g = c.three_gamma * m.mu;
+  const float usq3 = 3.0f * (m.ux * m.ux + m.uy * m.uy);
   const float S = ((g[1] + g[2]) + (g[3] + g[4])) + ((g[5] + g[6]) + (g[7] + g[8]));
-  dev_collide_dir<0>(c, m, base, ug, usq15, mu3g, d[0], g[0], S);
-  dev_collide_dir<1>(c, m, base, ug, usq15, mu3g, d[1], g[1], S);
-  dev_collide_dir<2>(c, m, base, ug, usq15, mu3g, d[2], g[2], S);
-  dev_collide_dir<3>(c, m, base, ug, usq15, mu3g, d[3], g[3], S);
-  dev_collide_dir<4>(c, m, base, ug, usq15, mu3g, d[4], g[4], S);
-  dev_collide_dir<5>(c, m, base, ug, usq15, mu3g, d[5], g[5], S);
-  dev_collide_dir<6>(c, m, base, ug, usq15, mu3g, d[6], g[6], S);
-  dev_collide_dir<7>(c, m, base, ug, usq15, mu3g, d[7], g[7], S);
-  dev_collide_dir<8>(c, m, base, ug, usq15, mu3g, d[8], g[8], S);
+  const float itg = c.inv_tau_g;
+  const float omt = 1.0f - m.inv_tau, omg = 1.0f - itg;
+  // rest direction: feq_0 - w0 = w0 (rho-1) - 3 (1-w0) psi mu - (w0 rho / 2) 3 u^2,
+  // F_0 = -3 w0 mu (1 - 1/(2 tau)) u.grad psi, geq_0 - g_0 = S - 3 (1-w0) gamma mu - (w0 psi / 2) 3 u^2
+  {
+    constexpr float w0 = wgt<0>();
+    const float deq = fmaf(w0, m.drho, fmaf(-0.5f * w0 * m.rho, usq3, -c.c_a0 * m.psi * m.mu));
+    const float F = -(3.0f * w0) * m.pref * ug;
+    d[0] = fmaf(deq - d[0], m.inv_tau, d[0]) + F;
+    const float dg = fmaf(-0.5f * w0 * m.psi, usq3, S - c.c_b0 * m.mu);
+    g[0] = fmaf(dg, itg, g[0]);
+  }
+  DevClass a;  // w = 1/9
+  a.yr = (1.0f / 9.0f) * m.inv_tau * m.rho;
+  a.xr = 0.5f * a.yr;
+  a.xb = (1.0f / 9.0f) * m.inv_tau * base;
+  a.P = (1.0f / 3.0f) * m.pref;
+  a.gt = ((1.0f / 9.0f) * itg) * m.psi;
+  a.gs = 0.5f * a.gt;
+  a.gc = ((1.0f / 9.0f) * itg) * c.three_gamma * m.mu;
+  DevClass b;  // w = 1/36 = (1/9) / 4
+  b.yr = 0.25f * a.yr;
+  b.xr = 0.25f * a.xr;
+  b.xb = 0.25f * a.xb;
+  b.P = 0.25f * a.P;
+  b.gt = 0.25f * a.gt;
+  b.gs = 0.25f * a.gs;
+  b.gc = 0.25f * a.gc;
+  dev_collide_pair<1>(m, a, usq3, ug, omt, omg, d[1], d[3], g[1], g[3]);
+  dev_collide_pair<2>(m, a, usq3, ug, omt, omg, d[2], d[4], g[2], g[4]);
+  dev_collide_pair<5>(m, b, usq3, ug, omt, omg, d[5], d[7], g[5], g[7]);
+  dev_collide_pair<6>(m, b, usq3, ug, omt, omg, d[6], d[8], g[6], g[8]);
 }
 
 // ---- Zou-He on deviations ----------------------------------------------------

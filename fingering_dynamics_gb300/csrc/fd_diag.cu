@@ -7,7 +7,10 @@
 //   mass_b = sum over fluid cells of rho (1 - psi) / 2   (defending fluid)
 //   invaded = number of fluid cells with psi > 0, saturation = invaded / fluid
 //   tip_x  = largest x of a fluid cell with psi > 0 (-1 if none)
-//   breakthrough = some fluid cell of column W-1 has psi > 0
+//   breakthrough = some fluid cell with x >= W-5 has psi > 0
+// (the outlet's Zou-He rule for g pins psi = -1 on column W-1, and the
+// mobility term pulls the columns next to it towards -1, so invading fluid
+// arriving at the outlet is seen in the last five columns, never in the last)
 // rho = sum f_i and psi = sum g_i are read from the stored populations: the
 // collision conserves both at every cell (sum of the forcing terms is zero,
 // fingering_periodic.py:194-199), so pre- and post-collision states give the
@@ -21,6 +24,7 @@ namespace {
 
 constexpr int kDiagThreads = 256;
 constexpr int kDiagBlocks = 1024;  // partials per reduction (fixed -> deterministic)
+constexpr int kOutletBand = 5;     // breakthrough columns: x >= W - kOutletBand
 
 struct Partial {
   double mass_r, mass_b;
@@ -83,7 +87,7 @@ __global__ void k_diag_partial(View v, const uint16_t* __restrict__ mask, int H,
       ++n;
       const int x = (int)(q % W);
       tip = max(tip, x);
-      if (x == W - 1) bt = 1;
+      if (x >= W - kOutletBand) bt = 1;
     }
   }
   const int t = threadIdx.x;

@@ -15,6 +15,8 @@ int check_storage(const fd_storage* s) {
              "packed storage supports FD_F32, FD_F16, FD_BF16 (got %d)", s->dtype);
   FD_REQUIRE(s->f_scale_log2 >= -30 && s->f_scale_log2 <= 30 && s->g_scale_log2 >= -30 && s->g_scale_log2 <= 30,
              FD_ERR_ARG, "storage scale exponents out of range");
+  FD_REQUIRE(s->rounding == FD_ROUND_NEAREST || s->rounding == FD_ROUND_STOCHASTIC, FD_ERR_ARG,
+             "storage rounding must be FD_ROUND_NEAREST or FD_ROUND_STOCHASTIC (got %d)", s->rounding);
   return FD_OK;
 }
 
@@ -113,17 +115,23 @@ int fd_fused_step_packed(const fd_params* prm, const fd_storage* st, const uint1
   const int R = rows_per_warp > 0 ? rows_per_warp : auto_rows_dev(prm->H, prm->W);
   float* sa = (float*)side_a;
   float* sb = (float*)side_b;
+  const bool sr = st->rounding == FD_ROUND_STOCHASTIC;
+  char* pa = (char*)pop_a;
+  char* pb = (char*)pop_b;
   int r;
   switch (st->dtype) {
     case FD_F16:
-      r = launch_fused_dev<__half, FD_DEV_VEC>(*prm, c, mask, inlet_ux, (char*)pop_a, (char*)pop_b, sa, sb, nsteps, R, s);
+      r = sr ? launch_fused_dev<__half, FD_DEV_VEC, true>(*prm, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, st->seed, s)
+             : launch_fused_dev<__half, FD_DEV_VEC, false>(*prm, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, 0, s);
       break;
     case FD_BF16:
-      r = launch_fused_dev<__nv_bfloat16, FD_DEV_VEC>(*prm, c, mask, inlet_ux, (char*)pop_a, (char*)pop_b, sa, sb,
-                                                      nsteps, R, s);
+      r = sr ? launch_fused_dev<__nv_bfloat16, FD_DEV_VEC, true>(*prm, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R,
+                                                                 st->seed, s)
+             : launch_fused_dev<__nv_bfloat16, FD_DEV_VEC, false>(*prm, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, 0,
+                                                                  s);
       break;
     default:
-      r = launch_fused_dev<float, FD_DEV_VEC>(*prm, c, mask, inlet_ux, (char*)pop_a, (char*)pop_b, sa, sb, nsteps, R, s);
+      r = launch_fused_dev<float, FD_DEV_VEC, false>(*prm, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, 0, s);
   }
   return r == FD_OK ? FD_OK : check_launch("fd_fused_step_packed");
 }

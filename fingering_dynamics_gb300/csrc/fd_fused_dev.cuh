@@ -39,6 +39,7 @@ struct DevArgs {
   SF* __restrict__ dst_gi;
   const float* __restrict__ side_in;
   float* __restrict__ side_out;
+  uint32_t seed;  // stochastic rounding: sr_hash of the step's seed
 };
 
 template <typename S, int VEC>
@@ -59,6 +60,18 @@ __device__ __forceinline__ void st_conv(S* __restrict__ p, float scale, const fl
   for (int k = 0; k < VEC; ++k) {
     if constexpr (std::is_same_v<S, float>) v[k] = in[k];
     else v[k] = from_f<S>(in[k] * scale);
+  }
+  st_vec<S, VEC>(p, v);
+}
+
+// st_conv with stochastic rounding; rs[k] is the random state of cell k
+template <typename S, int VEC>
+__device__ __forceinline__ void st_conv_sr(S* __restrict__ p, float scale, const float (&in)[VEC], uint32_t (&rs)[VEC]) {
+  S v[VEC];
+#pragma unroll
+  for (int k = 0; k < VEC; ++k) {
+    rs[k] = sr_next(rs[k]);
+    v[k] = from_f_sr<S>(in[k] * scale, rs[k]);
   }
   st_vec<S, VEC>(p, v);
 }
@@ -253,7 +266,7 @@ __device__ __forceinline__ void prefetch_rows(const DevArgs<SF>& a, int lane, in
   for (int i = 0; i < 8; ++i) issue(a.src_gi + i * a.pstride_f + rg, nf);
 }
 
-template <typename SF, int VEC>
+template <typename SF, int VEC, bool STOCH>
 __global__ void __launch_bounds__(128, FD_DEV_MINB) k_fused_dev(const DevArgs<SF> a) {
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -317,11 +330,22 @@ __global__ void __launch_bounds__(128, FD_DEV_MINB) k_fused_dev(const DevArgs<SF
     }
     if (owned) {
       const size_t row = (size_t)y * a.W + x0;
+      if constexpr (STOCH) {
+        uint32_t rs[VEC];
 #pragma unroll
-      for (int i = 0; i < 9; ++i) st_conv<SF, VEC>(a.dst_f + i * a.pstride_f + row, a.c.sf, f[i]);
-      st_conv<float, VEC>(a.dst_g0 + row, 1.0f, gC[0]);
+        for (int k = 0; k < VEC; ++k) rs[k] = sr_hash((uint32_t)(row + k) ^ a.seed);
 #pragma unroll
-      for (int i = 1; i < 9; ++i) st_conv<SF, VEC>(a.dst_gi + (i - 1) * a.pstride_f + row, a.c.sg, gC[i]);
+        for (int i = 0; i < 9; ++i) st_conv_sr<SF, VEC>(a.dst_f + i * a.pstride_f + row, a.c.sf, f[i], rs);
+        st_conv<float, VEC>(a.dst_g0 + row, 1.0f, gC[0]);
+#pragma unroll
+        for (int i = 1; i < 9; ++i) st_conv_sr<SF, VEC>(a.dst_gi + (i - 1) * a.pstride_f + row, a.c.sg, gC[i], rs);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) st_conv<SF, VEC>(a.dst_f + i * a.pstride_f + row, a.c.sf, f[i]);
+        st_conv<float, VEC>(a.dst_g0 + row, 1.0f, gC[0]);
+#pragma unroll
+        for (int i = 1; i < 9; ++i) st_conv<SF, VEC>(a.dst_gi + (i - 1) * a.pstride_f + row, a.c.sg, gC[i]);
+      }
     }
 #pragma unroll
     for (int k = 0; k < VEC; ++k) {
@@ -379,9 +403,9 @@ inline PackedLayout<SF> packed_layout(int H, int W) {
   return L;
 }
 
-template <typename SF, int VEC>
+template <typename SF, int VEC, bool STOCH>
 int launch_fused_dev(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, char* pa,
-                     char* pb, float* sa, float* sb, int nsteps, int R, cudaStream_t st) {
+                     char* pb, float* sa, float* sb, int nsteps, int R, uint32_t seed, cudaStream_t st) {
   const PackedLayout<SF> L = packed_layout<SF>(p.H, p.W);
   DevArgs<SF> a;
   a.c = c;
@@ -408,7 +432,8 @@ int launch_fused_dev(const fd_params& p, const DevCoef& c, const uint16_t* mask,
     a.dst_gi = reinterpret_cast<SF*>(dst + L.off_gi);
     a.side_in = (s % 2 == 0) ? sa : sb;
     a.side_out = (s % 2 == 0) ? sb : sa;
-    k_fused_dev<SF, VEC><<<blocks, 128, 0, st>>>(a);
+    a.seed = sr_hash(seed + (uint32_t)s);
+    k_fused_dev<SF, VEC, STOCH><<<blocks, 128, 0, st>>>(a);
   }
   return cudaGetLastError() == cudaSuccess ? FD_OK : FD_ERR_CUDA;
 }

@@ -12,15 +12,23 @@
 
 namespace fd {
 
-template <typename SF>
-int fused_tma_t(const fd_params& p, const fd_storage& st, const DevCoef& c, const uint16_t* mask,
+template <typename SF, bool STOCH>
+int fused_tma_r(const fd_params& p, const fd_storage& st, const DevCoef& c, const uint16_t* mask,
                 const double* inlet_ux, void* pa, void* pb, void* sa, void* sb, int nsteps, int R, cudaStream_t s) {
   const bool scaled = st.f_scale_log2 != 0 || st.g_scale_log2 != 0;
   if (scaled)
-    return launch_fused_tma<SF, FD_TMA_NT, FD_TMA_NS, true>(p, c, mask, inlet_ux, (char*)pa, (char*)pb, (float*)sa,
-                                                            (float*)sb, nsteps, R, s);
-  return launch_fused_tma<SF, FD_TMA_NT, FD_TMA_NS, false>(p, c, mask, inlet_ux, (char*)pa, (char*)pb, (float*)sa,
-                                                           (float*)sb, nsteps, R, s);
+    return launch_fused_tma<SF, FD_TMA_NT, FD_TMA_NS, true, STOCH>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
+                                                                   (float*)sa, (float*)sb, nsteps, R, st.seed, s);
+  return launch_fused_tma<SF, FD_TMA_NT, FD_TMA_NS, false, STOCH>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
+                                                                  (float*)sa, (float*)sb, nsteps, R, st.seed, s);
+}
+
+template <typename SF>
+int fused_tma_t(const fd_params& p, const fd_storage& st, const DevCoef& c, const uint16_t* mask,
+                const double* inlet_ux, void* pa, void* pb, void* sa, void* sb, int nsteps, int R, cudaStream_t s) {
+  if (st.rounding == FD_ROUND_STOCHASTIC)
+    return fused_tma_r<SF, true>(p, st, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, s);
+  return fused_tma_r<SF, false>(p, st, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, s);
 }
 
 int fused_tma(const fd_params& p, const fd_storage& st, const DevCoef& c, const uint16_t* mask,
@@ -29,8 +37,8 @@ int fused_tma(const fd_params& p, const fd_storage& st, const DevCoef& c, const 
     case FD_F16: return fused_tma_t<__half>(p, st, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, s);
     case FD_BF16: return fused_tma_t<__nv_bfloat16>(p, st, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, s);
     default:
-      return launch_fused_tma<float, FD_TMA_NT, FD_TMA_NS, false>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
-                                                                  (float*)sa, (float*)sb, nsteps, R, s);
+      return launch_fused_tma<float, FD_TMA_NT, FD_TMA_NS, false, false>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
+                                                                         (float*)sa, (float*)sb, nsteps, R, 0, s);
   }
 }
 

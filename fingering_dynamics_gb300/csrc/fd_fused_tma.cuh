@@ -179,7 +179,7 @@ __device__ __forceinline__ float psi_cell(const char* sm, const DevArgs<SF>& a, 
 // batched persistent kernel.  The mbarriers must be initialised; `phase`
 // (per-slot parity of the next fill to wait for) and `ok` carry over from
 // strip to strip.  Ends with a CTA barrier, so the ring can be refilled.
-template <typename SF, int NT, int NS, bool SCALED>
+template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int strip, char* smem, unsigned& phase,
                                           bool& ok) {
   static_assert(NS == 5, "the slot rotation below keeps rows y-2 .. y+2 in five slots");
@@ -195,10 +195,10 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
   const bool owned = x < a.W;
   const bool walls = a.variant == FD_VARIANT_WALLS;
   const int first = y0 - 2, last = y1 + 1;  // ring rows: y0-2 .. y1+1
-  // halo cells of the band: the left one by thread 0, the right one by the
-  // last thread (different warps share the extra work)
-  const int hl = (t == 0) ? -1 : (t == NT - 1 ? NT : 0);
-  const bool halo = (t == 0) || (t == NT - 1);
+  // halo cells of the band: the left one by thread NT/2, the right one by
+  // the last thread (warp 0 issues the copies; other warps take the halos)
+  const int hl = (t == NT / 2) ? -1 : (t == NT - 1 ? NT : 0);
+  const bool halo = (t == NT / 2) || (t == NT - 1);
 
   // row first + k lives in slot k (mod 5); rows y0-2 .. y0+2 fill slots 0..4
   if (t == 0) {
@@ -220,6 +220,7 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
   auto psi_row = [&](int k) { return psi_ring + ((pslot + k) & 3) * M::PSI_ROW; };
 
   float gC[9], gN[9];
+  float pS = 0.0f, pC = 0.0f;  // psi of this column at rows y-1 and y
   // prologue: psi of rows y0-1 and y0 (needs rows y0-2 .. y0+1)
   wait_slot(0);
   wait_slot(1);
@@ -232,7 +233,10 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
     float* pr = psi_row(k);
     const bool ghost = walls && (r < 0 || r >= a.H);
     const int yr = wrap(r, a.H);
-    pr[t + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x, t, yr, gN);
+    const float pv = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x, t, yr, gN);
+    pr[t + 1] = pv;
+    if (k == 0) pS = pv;
+    else pC = pv;
     if (halo) {
       float gh[9];
       pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x0 + hl, hl, yr, gh);
@@ -243,13 +247,15 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
 
   for (int y = y0; y < y1; ++y) {
     // 1. psi of row y+1 from rows y, y+1, y+2
+    float pN;
     wait_slot(si[4]);
     {
       const int rows[3] = {so[2], so[3], so[4]};
       const bool ghost = walls && (y + 1 >= a.H);
       const int yr = wrap(y + 1, a.H);
       float* pr = psi_row(2);
-      pr[t + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x, t, yr, gN);
+      pN = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x, t, yr, gN);
+      pr[t + 1] = pN;
       if (halo) {
         float gh[9];
         pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x0 + hl, hl, yr, gh);
@@ -275,7 +281,7 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
       const float* pc = psi_row(1);
       const float* pn = psi_row(2);
       const int j = t + 1;
-      const float C = pc[j], E = pc[j + 1], Wv = pc[j - 1], N = pn[j], S = pm[j];
+      const float C = pC, E = pc[j + 1], Wv = pc[j - 1], N = pN, S = pS;
       const float NE = pn[j + 1], NW = pn[j - 1], SE = pm[j + 1], SW = pm[j - 1];
       const float gx = (4.0f * (E - Wv) + ((NE - NW) + (SE - SW))) * (1.0f / 12.0f);
       const float gy = (4.0f * (N - S) + ((NE + NW) - (SE + SW))) * (1.0f / 12.0f);
@@ -297,24 +303,33 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
         dev_collide(a.c, mc, f, gC);
       }
       const size_t q = (size_t)y * a.W + x;
+      uint32_t rs = 0;  // stochastic rounding state of this cell (fd_dev.cuh)
+      if constexpr (STOCH) rs = sr_hash((uint32_t)q ^ a.seed);
+      auto put = [&](SF* p, float v, float scale) {
+        if constexpr (std::is_same_v<SF, float>) {
+          *p = v;
+        } else {
+          if constexpr (SCALED) v *= scale;
+          if constexpr (STOCH) {
+            rs = sr_next(rs);
+            *p = from_f_sr<SF>(v, rs);
+          } else {
+            *p = from_f<SF>(v);
+          }
+        }
+      };
       SF* pf = a.dst_f + q;
 #pragma unroll
-      for (int i = 0; i < 9; ++i, pf += a.pstride_f) {
-        if constexpr (std::is_same_v<SF, float>) *pf = f[i];
-        else if constexpr (SCALED) *pf = from_f<SF>(f[i] * a.c.sf);
-        else *pf = from_f<SF>(f[i]);
-      }
+      for (int i = 0; i < 9; ++i, pf += a.pstride_f) put(pf, f[i], a.c.sf);
       a.dst_g0[q] = gC[0];
       SF* pg = a.dst_gi + q;
 #pragma unroll
-      for (int i = 1; i < 9; ++i, pg += a.pstride_f) {
-        if constexpr (std::is_same_v<SF, float>) *pg = gC[i];
-        else if constexpr (SCALED) *pg = from_f<SF>(gC[i] * a.c.sg);
-        else *pg = from_f<SF>(gC[i]);
-      }
+      for (int i = 1; i < 9; ++i, pg += a.pstride_f) put(pg, gC[i], a.c.sg);
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) gC[i] = gN[i];
+    pS = pC;
+    pC = pN;
     // rotate: rows y-1 .. y+3 become y-2 .. y+2 for the next row
     const int freed = si[0], freed_off = so[0];
 #pragma unroll
@@ -350,13 +365,13 @@ __device__ __forceinline__ void init_ring(char* smem) {
   __syncthreads();
 }
 
-template <typename SF, int NT, int NS, bool SCALED>
+template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 __global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nbands) {
   extern __shared__ __align__(128) char smem[];
   init_ring<SF, NT, NS>(smem);
   unsigned phase = 0;
   bool ok = true;
-  tma_strip<SF, NT, NS, SCALED>(a, (int)blockIdx.x % nbands, (int)blockIdx.x / nbands, smem, phase, ok);
+  tma_strip<SF, NT, NS, SCALED, STOCH>(a, (int)blockIdx.x % nbands, (int)blockIdx.x / nbands, smem, phase, ok);
 }
 
 // One lattice of a batch: its arguments for both ping-pong parities.
@@ -367,19 +382,35 @@ struct BatchInst {
 
 // Persistent kernel over a tile table of (instance, band, strip) entries: CTA
 // b takes tiles b, b + gridDim.x, ...  Every instance advances one iteration.
-template <typename SF, int NT, int NS, bool SCALED>
+//
+// Step counter for stochastic rounding: `steps` holds two slots; the launch of
+// parity p reads slot p (the number of batch steps done so far) and one
+// thread writes slot 1-p = slot p + 1 for the next launch.  A launch never
+// writes the slot it reads, and launches on a stream are ordered, so the
+// sequence is deterministic and advances under CUDA-graph replay too.  A
+// member's step seed is its own seed (args.seed) plus the counter.
+template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 __global__ void __launch_bounds__(NT) k_fused_tma_batch(const BatchInst<SF>* __restrict__ inst,
-                                                        const int4* __restrict__ tiles, int ntiles, int parity) {
+                                                        const int4* __restrict__ tiles, int ntiles, int parity,
+                                                        unsigned* __restrict__ steps) {
   extern __shared__ __align__(128) char smem[];
   __shared__ DevArgs<SF> sa;
   init_ring<SF, NT, NS>(smem);
+  unsigned done = 0;
+  if constexpr (STOCH) {
+    done = steps[parity];
+    if (blockIdx.x == 0 && threadIdx.x == 0) steps[parity ^ 1] = done + 1;
+  }
   unsigned phase = 0;
   bool ok = true;
   for (int k = blockIdx.x; k < ntiles && ok; k += gridDim.x) {
     const int4 tl = tiles[k];
-    if (threadIdx.x == 0) sa = inst[tl.x].args[parity];
+    if (threadIdx.x == 0) {
+      sa = inst[tl.x].args[parity];
+      if constexpr (STOCH) sa.seed = sr_hash(sa.seed + done);
+    }
     __syncthreads();
-    tma_strip<SF, NT, NS, SCALED>(sa, tl.y, tl.z, smem, phase, ok);
+    tma_strip<SF, NT, NS, SCALED, STOCH>(sa, tl.y, tl.z, smem, phase, ok);
   }
 }
 
@@ -387,14 +418,14 @@ __global__ void __launch_bounds__(NT) k_fused_tma_batch(const BatchInst<SF>* __r
 
 namespace fd {
 
-template <typename SF, int NT, int NS, bool SCALED>
+template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, char* pa,
-                     char* pb, float* sa, float* sb, int nsteps, int R, cudaStream_t st) {
+                     char* pb, float* sa, float* sb, int nsteps, int R, uint32_t seed, cudaStream_t st) {
   using M = TmaSmem<SF, NT, NS>;
   static bool attr_set = false;
   if (!attr_set) {
-    if (cudaFuncSetAttribute(k_fused_tma<SF, NT, NS, SCALED>, cudaFuncAttributeMaxDynamicSharedMemorySize, M::BYTES) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(k_fused_tma<SF, NT, NS, SCALED, STOCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             M::BYTES) != cudaSuccess)
       return FD_ERR_CUDA;
     attr_set = true;
   }
@@ -411,7 +442,7 @@ int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask,
   const int nbands = (p.W + NT - 1) / NT;
   if (R <= 0) {
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tma<SF, NT, NS, SCALED>, NT, M::BYTES);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tma<SF, NT, NS, SCALED, STOCH>, NT, M::BYTES);
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -436,7 +467,8 @@ int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask,
     a.dst_gi = reinterpret_cast<SF*>(dst + L.off_gi);
     a.side_in = (s % 2 == 0) ? sa : sb;
     a.side_out = (s % 2 == 0) ? sb : sa;
-    k_fused_tma<SF, NT, NS, SCALED><<<blocks, NT, M::BYTES, st>>>(a, nbands);
+    a.seed = sr_hash(seed + (uint32_t)s);
+    k_fused_tma<SF, NT, NS, SCALED, STOCH><<<blocks, NT, M::BYTES, st>>>(a, nbands);
   }
   return cudaGetLastError() == cudaSuccess ? FD_OK : FD_ERR_CUDA;
 }

@@ -91,10 +91,14 @@ class Ensemble:
     """Independent lattices advanced by one batched launch per iteration."""
 
     def __init__(self, members, dtype: str = "f32", rows_per_strip: int = 32, band_width: int = 128,
-                 device="cuda"):
-        """members: (LBMParams, Geometry) or (LBMParams, Geometry, initial psi) tuples."""
-        self.lattices = [Lattice(m[0], m[1], dtype=dtype, device=device, psi0=m[2] if len(m) > 2 else None)
-                         for m in members]
+                 device="cuda", rounding: str = "stochastic"):
+        """members: (LBMParams, Geometry) or (LBMParams, Geometry, initial psi) tuples.
+        ``rounding``: FP16/BF16 store rounding (stochastic by default); member
+        k's stochastic-rounding seed is k, its steps use seed + iteration as
+        they would when advanced alone."""
+        self.lattices = [Lattice(m[0], m[1], dtype=dtype, device=device, psi0=m[2] if len(m) > 2 else None,
+                                 rounding=rounding, seed=k)
+                         for k, m in enumerate(members)]
         for lat in self.lattices:
             if lat.storage is None:
                 raise ValueError("ensembles use packed storage: dtype f32, f16 or bf16")
@@ -106,7 +110,8 @@ class Ensemble:
         for k, lat in enumerate(self.lattices):
             arr[k] = L.fd_instance(lat.prm, lat.mask.data_ptr(), lat.inlet_ux.data_ptr(),
                                    lat.ppop[lat.pcur].data_ptr(), lat.ppop[1 - lat.pcur].data_ptr(),
-                                   lat.side[lat.scur].data_ptr(), lat.side[1 - lat.scur].data_ptr())
+                                   lat.side[lat.scur].data_ptr(), lat.side[1 - lat.scur].data_ptr(),
+                                   lat.step_seed())
         self._inst = arr
         self._batch = C.c_void_p()
         L.call("fd_batch_create", arr, n, C.byref(self.lattices[0].storage), int(rows_per_strip), int(band_width),

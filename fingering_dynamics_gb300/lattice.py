@@ -35,7 +35,8 @@ from .params import LBMParams
 # name -> (reference-layout torch dtype, reference-layout fd dtype, packed storage or None)
 #   f64        FP64 everywhere; the fused kernel reproduces the reference bit for bit
 #   f32        FP32 reference-order kernels; fused kernel in deviation form, FP32 storage
-#   f16 / bf16 as f32, fused storage of f deviations and g_1..g_8 in FP16 / BF16 (g_0 FP32)
+#   f16 / bf16 as f32, fused storage of f deviations and g_1..g_8 in FP16 / BF16 (g_0 FP32),
+#              stochastic rounding by default (``rounding="nearest"`` for round to nearest even)
 #   f32-exact  FP32 with the reference's operand order in the fused kernel too
 DTYPES = {
     "f64": (torch.float64, L.FD_F64, None),
@@ -61,7 +62,12 @@ class Lattice:
     """One two-phase D2Q9 simulation resident on a GPU."""
 
     def __init__(self, params: LBMParams, geometry: Geometry, dtype: str = "f64", device="cuda",
-                 rho0: np.ndarray | None = None, psi0: np.ndarray | None = None):
+                 rho0: np.ndarray | None = None, psi0: np.ndarray | None = None, rounding: str = "stochastic",
+                 seed: int = 0):
+        """``rounding`` / ``seed``: rounding of the FP16/BF16 stores of the
+        fused step (include/fdlbm.h ``fd_storage``); the step at iteration k
+        uses seed + k, so a run is reproducible and a resumed run continues
+        bit for bit."""
         if dtype not in DTYPES:
             raise ValueError(f"dtype must be one of {sorted(DTYPES)}")
         if (geometry.H, geometry.W) != (params.H, params.W):
@@ -70,7 +76,11 @@ class Lattice:
         self.geometry = geometry
         self.dtype = dtype
         self.tdtype, self.fd_dtype, packed = DTYPES[dtype]
-        self.storage = None if packed is None else L.fd_storage(*packed)
+        if rounding not in L.ROUNDING:
+            raise ValueError(f"rounding must be one of {sorted(L.ROUNDING)}")
+        self.rounding = rounding
+        self.seed = int(seed) & 0xFFFFFFFF
+        self.storage = None if packed is None else L.fd_storage(*packed, L.ROUNDING[rounding], 0)
         if torch.device(device).type != "cuda":
             raise ValueError("Lattice runs on a CUDA device only")
         self.device = torch.empty(0, device=device).device  # concrete index, e.g. cuda:0
@@ -193,6 +203,7 @@ class Lattice:
                 self.cur = 1 - self.cur
         else:
             a, b = self.ppop[self.pcur], self.ppop[1 - self.pcur]
+            self.storage.seed = self.step_seed()
             L.call("fd_fused_step_packed", C.byref(self.prm), C.byref(self.storage), _ptr(self.mask),
                    _ptr(self.inlet_ux), _ptr(a), _ptr(b), _ptr(sa), _ptr(sb), int(n), int(rows_per_warp),
                    self._stream())
@@ -201,6 +212,10 @@ class Lattice:
         if n % 2:
             self.scur = 1 - self.scur
         self.iteration += n
+
+    def step_seed(self) -> int:
+        """Stochastic-rounding seed of the next fused launch."""
+        return (self.seed + self.iteration) & 0xFFFFFFFF
 
     def exit_fused(self):
         """Finish the pending iteration; the fields become current."""
@@ -255,7 +270,8 @@ class Lattice:
         torch.cuda.current_stream(self.device).synchronize()
         rec = {"mode": np.array(self.mode), "iteration": np.array(self.iteration), "dtype": np.array(self.dtype),
                "H": np.array(self.H), "W": np.array(self.W), "mask_word": self.geometry.mask_word,
-               "state": self.current_buffer().cpu().numpy(), "side": self.side[self.scur].cpu().numpy()}
+               "state": self.current_buffer().cpu().numpy(), "side": self.side[self.scur].cpu().numpy(),
+               "rounding": np.array(self.rounding), "seed": np.array(self.seed, dtype=np.uint32)}
         if self.mode == "reference":
             for n in FIELD_NAMES:
                 rec[n] = getattr(self, n).cpu().numpy()
@@ -275,6 +291,11 @@ class Lattice:
                 self.enter_fused()  # allocates the packed buffers
             self.mode = mode
             self.iteration = int(z["iteration"])
+            if "seed" in z.files:  # the stochastic-rounding stream continues where it stopped
+                self.seed = int(z["seed"])
+                self.rounding = str(z["rounding"])
+                if self.storage is not None:
+                    self.storage.rounding = L.ROUNDING[self.rounding]
             self.current_buffer().copy_(torch.from_numpy(z["state"]))
             self.side[self.scur].copy_(torch.from_numpy(z["side"]))
             if mode == "reference":

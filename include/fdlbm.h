@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define FDLBM_ABI_VERSION 1
+#define FDLBM_ABI_VERSION 2
 
 enum fd_status {
   FD_OK = 0,
@@ -201,11 +201,24 @@ int fd_fused_step(const fd_params* prm, int dtype, const uint16_t* mask, const d
  * in `dtype` (FD_F32, FD_F16 or FD_BF16); g_0, which carries most of psi, is
  * always FP32.  Arithmetic is FP32 in every case.  The layout is 18 planes of
  * H*W elements, each starting on a 256-byte boundary: f_0..f_8, g_0, g_1..g_8.
- * There is no counterpart in the reference (it stores float64 only). */
+ * There is no counterpart in the reference (it stores float64 only).
+ *
+ * Rounding of the FP16/BF16 stores of the fused step: FD_ROUND_NEAREST
+ * (round to nearest even) or FD_ROUND_STOCHASTIC (round up with probability
+ * equal to the discarded fraction, from a counter-based hash of the cell index
+ * and the step's seed).  Round-to-nearest makes the same error in every cell
+ * of a uniform region at every step, so the error accumulates as a drift of
+ * the colour masses; stochastic rounding makes it zero-mean.  Step s of a call
+ * (s = 0 .. nsteps-1) uses seed + s; results are reproducible for a given
+ * seed.  pack/unpack always round to nearest; FD_F32 ignores both fields. */
+enum fd_rounding { FD_ROUND_NEAREST = 0, FD_ROUND_STOCHASTIC = 1 };
+
 typedef struct fd_storage {
   int32_t dtype;
   int32_t f_scale_log2;
   int32_t g_scale_log2;
+  int32_t rounding;   /* fd_rounding */
+  uint32_t seed;      /* stochastic rounding: seed of the first step of a call */
 } fd_storage;
 
 /* Bytes of one packed population buffer (0 on invalid arguments). */
@@ -254,6 +267,8 @@ typedef struct fd_instance {
   void* pop_b;
   void* side_a;             /* device, 6*H floats: the state's boundary values at parity 0 */
   void* side_b;
+  uint32_t seed;            /* stochastic rounding: seed of the batch's first step for this member;
+                               batch step k uses seed + k, as fd_fused_step_packed would */
 } fd_instance;
 
 typedef struct fd_batch fd_batch;
@@ -292,7 +307,8 @@ typedef struct fd_diag {
   int64_t invaded;      /* fluid cells with psi > 0 */
   int64_t fluid;        /* fluid cells */
   int32_t tip_x;        /* largest x of a fluid cell with psi > 0, -1 if none */
-  int32_t breakthrough; /* 1 if a fluid cell of column W-1 has psi > 0 */
+  int32_t breakthrough; /* 1 if a fluid cell with x >= W-5 has psi > 0 (the outlet rule pins
+                           psi = -1 on column W-1 itself) */
 } fd_diag;
 
 /* Bytes of the scratch buffer fd_diagnostics needs (independent of the size). */

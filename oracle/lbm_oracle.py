@@ -445,5 +445,5 @@ def diagnostics(st: OracleState) -> dict:
         "fluid": int(m.sum()),
         "saturation": float(inv.sum() / max(int(m.sum()), 1)),
         "tip_x": int(xs[inv].max()) if inv.any() else -1,
-        "breakthrough": int(bool(inv[xs == st.prm.W - 1].any())),
+        "breakthrough": int(bool(inv[xs >= st.prm.W - 5].any())),
     }

@@ -39,7 +39,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_abi_version_and_error_path(lib):
     from fingering_dynamics_gb300 import _lib as L
-    assert L.lib().fd_abi_version() == 1
+    assert L.lib().fd_abi_version() == 2
     # host-side argument checks run without a GPU and report through fd_last_error
     with pytest.raises(L.FDError) as e:
         L.call("fd_fused_step", None, 1, None, None, None, None, None, None, 1, 0, None)

@@ -27,7 +27,7 @@ def test_batch_equals_single_lattices(dtype):
     from fingering_dynamics_gb300.lattice import Lattice
     members = _members()
     ens = Ensemble(members, dtype=dtype, rows_per_strip=16, band_width=64)
-    singles = [Lattice(p, g, dtype=dtype) for p, g in members]
+    singles = [Lattice(p, g, dtype=dtype, seed=k) for k, (p, g) in enumerate(members)]
     for s in singles:
         s.enter_fused()
     ens.step(3, use_graph=False)

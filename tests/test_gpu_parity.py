@@ -29,7 +29,7 @@ def _built():
     build.build()
 
 
-def make_lattice(fx, dtype):
+def make_lattice(fx, dtype, **kw):
     from fingering_dynamics_gb300 import geometry as geo
     from fingering_dynamics_gb300.lattice import Lattice
     prm = lbm_params(fx)
@@ -38,7 +38,7 @@ def make_lattice(fx, dtype):
     circles = [((int(c[0]), int(c[1])), int(c[2])) for c in fx["circles"]]
     g = geo.build_geometry(H, W, rects=rects, circles=circles, walls=prm.variant == "walls")
     _, rho0, _, _ = fixture_geometry(fx)
-    return Lattice(prm, g, dtype=dtype, device="cuda", rho0=rho0)
+    return Lattice(prm, g, dtype=dtype, device="cuda", rho0=rho0, **kw)
 
 
 def _eq(a, b):
@@ -192,14 +192,16 @@ def test_fused_500_steps_fp32_exact_order(name):
 
 # max |d psi| after 500 steps against the reference's FP64 run: FP16 storage
 # meets 1e-3; BF16 (8-bit significand) is held to the error it shows, 5e-2
+# (both with stochastic and with round-to-nearest stores)
 REDUCED_PSI_TOL = {"f16": 1e-3, "bf16": 5e-2}
 
 
+@pytest.mark.parametrize("rounding", ["stochastic", "nearest"])
 @pytest.mark.parametrize("dtype", ["f16", "bf16"])
 @pytest.mark.parametrize("name", LONG)
-def test_fused_500_steps_reduced_precision(name, dtype):
+def test_fused_500_steps_reduced_precision(name, dtype, rounding):
     fx = load(name)
-    lat = make_lattice(fx, dtype)
+    lat = make_lattice(fx, dtype, rounding=rounding)
     lat.step(500)
     st = lat.state()
     m = np.isfinite(fx["s500_rho"])
@@ -207,6 +209,84 @@ def test_fused_500_steps_reduced_precision(name, dtype):
     assert dpsi <= REDUCED_PSI_TOL[dtype], dpsi
     err = _rel_errors(st, fx)
     assert err["rho_r"] <= 10 * REDUCED_PSI_TOL[dtype] and err["rho_b"] <= 10 * REDUCED_PSI_TOL[dtype], err
+
+
+@pytest.mark.parametrize("dtype", ["f16", "bf16"])
+def test_stochastic_rounding_is_reproducible(dtype):
+    """Same seed -> bit-identical states; another seed -> a different state;
+    stepping 7 + 5 equals stepping 12 (the seed follows the iteration)."""
+    fx = load("walls_rects_24x48")
+    runs = []
+    for seed, split in ((3, (12,)), (3, (7, 5)), (4, (12,))):
+        lat = make_lattice(fx, dtype, seed=seed)
+        lat.enter_fused()
+        for n in split:
+            lat.advance(n)
+        torch.cuda.synchronize()
+        runs.append(lat.current_buffer().clone())
+    assert torch.equal(runs[0], runs[1])
+    assert not torch.equal(runs[0], runs[2])
+
+
+def _g1_plane(lat):
+    """g_1 of the packed state as float32 (H, W)."""
+    P = lat.H * lat.W
+    buf = lat.ppop[lat.pcur]
+    es = 2 if lat.dtype in ("f16", "bf16") else 4
+    plane = (P * es + 255) // 256 * 256
+    start = 9 * plane + (P * 4 + 255) // 256 * 256
+    raw = buf[start:start + P * es]
+    if lat.dtype == "f16":
+        return raw.view(torch.float16).float().view(lat.H, lat.W)
+    return raw.view(torch.float32).view(lat.H, lat.W)
+
+
+def test_stochastic_rounding_is_unbiased():
+    """A uniform state (psi = 0.3337, off the well minimum; u = 0) stepped
+    once from FP16 storage: every interior cell computes the same FP32 value of
+    g_1, which an FP32-storage lattice started from the same (exactly widened)
+    state stores as is.  Round to nearest stores one FP16 value everywhere (a
+    fixed error per step); stochastic rounding stores the two neighbouring FP16
+    values with mean equal to the FP32 value within the sampling error."""
+    import ctypes as C
+    from fingering_dynamics_gb300 import _lib as L
+    from fingering_dynamics_gb300 import geometry as geo
+    from fingering_dynamics_gb300.lattice import Lattice
+    from fingering_dynamics_gb300.params import periodic_reference_params
+    H, W = 256, 512
+    prm = periodic_reference_params().with_size(H, W)
+    prm.inlet_ux = np.zeros(H)
+    g = geo.build_geometry(H, W)
+    psi0 = np.full((H, W), 0.3337)
+    vals = {}
+    for rounding in ("nearest", "stochastic"):
+        l16 = Lattice(prm, g, dtype="f16", psi0=psi0, rounding=rounding, seed=5)
+        l16.enter_fused()
+        if rounding == "nearest":
+            # the same packed input, widened exactly, in FP32 storage
+            l32 = Lattice(prm, g, dtype="f32", psi0=psi0)
+            l32.enter_fused()
+            tmp = torch.empty((18, H, W), dtype=torch.float32, device="cuda")
+            L.call("fd_unpack", C.byref(l16.prm), C.byref(l16.storage), C.c_void_p(l16.ppop[l16.pcur].data_ptr()),
+                   L.FD_F32, C.c_void_p(tmp.data_ptr()), None)
+            L.call("fd_pack", C.byref(l32.prm), L.FD_F32, C.c_void_p(tmp.data_ptr()), C.byref(l32.storage),
+                   C.c_void_p(l32.ppop[l32.pcur].data_ptr()), None)
+            l32.side[l32.scur].copy_(l16.side[l16.scur])
+            l32.advance(1)
+            torch.cuda.synchronize()
+            vals["f32"] = _g1_plane(l32)[16:-16, 16:-16].double()
+        l16.advance(1)
+        torch.cuda.synchronize()
+        vals[rounding] = _g1_plane(l16)[16:-16, 16:-16].double()
+    ref = vals["f32"]
+    exact = ref[0, 0].item()
+    assert torch.all(ref == exact)
+    rn = vals["nearest"]
+    assert torch.all(rn == rn[0, 0])
+    sr = vals["stochastic"]
+    n = sr.numel()
+    assert sr.std().item() > 0 and len(torch.unique(sr)) == 2
+    assert abs(sr.mean().item() - exact) < 5 * sr.std().item() / n ** 0.5
 
 
 @pytest.mark.parametrize("dtype", ["f32", "f16", "bf16"])
