@@ -226,7 +226,7 @@ def run_ours(args):
     from fingering_dynamics_gb300.lattice import Lattice
     build.build()
     prm, g = workload(args.H, args.W, seed=2024 + rank)
-    lat = Lattice(prm, g, dtype=args.dtype, device=f"cuda:{local}")
+    lat = Lattice(prm, g, dtype=args.dtype, device=f"cuda:{local}", rounding=args.rounding)
     H, W = prm.H, prm.W
     lat.enter_fused()
     for _ in range(args.warmup):
@@ -295,6 +295,7 @@ def run_ours(args):
                        "tau_inv": TAU_INV, "tau_def": 1.0, "sigma": 5e-4, "contact_angle_deg": 120, "u_in": 0.01,
                        "l2": "inputs larger than L2 (populations 2 x %d MB)" % (pop_bytes // 2 ** 20),
                        "parallelism": f"replicas{world}", "rows_per_warp": args.rows or "auto",
+                       "rounding": args.rounding if args.dtype in ("f16", "bf16") else None,
                        "state_finite_after_timing": finite},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
@@ -323,7 +324,7 @@ def run_ensemble(args):
     from fingering_dynamics_gb300.ensemble import Ensemble, ensemble_specs
     build.build()
     specs = ensemble_specs(args.members, seed=2024, family=args.family)
-    ens = Ensemble([s.build() for s in specs], dtype=args.dtype)
+    ens = Ensemble([s.build() for s in specs], dtype=args.dtype, rounding=args.rounding)
     tuned = ens.autotune(steps=10)
     for _ in range(args.warmup):
         ens.step(1)
@@ -343,6 +344,7 @@ def run_ensemble(args):
             "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
             "config": {"workload": f"ensemble_{args.members}_members", "members": args.members, "cells": ens.cells,
                        "family": args.family,
+                       "rounding": args.rounding if args.dtype in ("f16", "bf16") else None,
                        "tile_shape": {"band_width": ens.config[0], "rows_per_strip": ens.config[1]},
                        "autotune_mlups": {f"{b}x{r}": round(v, 1) for (b, r), v in tuned.items()},
                        "tiles_per_iteration": ens.tiles, "members_finite_after_timing": int(sum(finite)),
@@ -398,6 +400,8 @@ def main():
     ap.add_argument("--workload", default="single", choices=["single", "ensemble", "precision"],
                     help="single 4096 x 2048 lattice (default), the batched ensemble, or the error study of "
                          "reduced-precision storage against the FP64 path (1024 x 256, --steps iterations)")
+    ap.add_argument("--rounding", default="stochastic", choices=["stochastic", "nearest"],
+                    help="rounding of FP16/BF16 population stores")
     ap.add_argument("--every", type=int, default=500, help="precision study: iterations between comparisons")
     ap.add_argument("--out", default=None, help="precision study: write the full curves to this JSON file")
     ap.add_argument("--members", type=int, default=96, help="ensemble members")

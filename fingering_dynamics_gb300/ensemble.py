@@ -65,15 +65,27 @@ class MemberSpec:
 
 
 def ensemble_specs(n: int, seed: int, sizes_w=(256, 512, 1024, 2048), sizes_h=(128, 256, 512),
-                   porosity=(0.6, 0.85), ratio=None, angle=(30.0, 150.0), sigma=(1e-4, 1e-3),
-                   u_in=(0.005, 0.02), family: str = "stable", psi_wall=(-1.0, -0.5)) -> list[MemberSpec]:
+                   porosity=None, ratio=None, angle=(30.0, 150.0), sigma=(1e-4, 1e-3),
+                   u_in=None, family: str = "stable", psi_wall=(-1.0, -0.5)) -> list[MemberSpec]:
     """n members drawn from a seeded generator: sizes uniform over the given
     widths x heights, porosity uniform, viscosity ratio and interfacial
     tension log-uniform, contact angle, psi_wall and inlet speed uniform.
-    The viscosity ratio defaults to 2..20 for family "spec" (the batched
-    ensemble of the benchmark configuration) and 2..5 for "stable"."""
+
+    Family "spec" defaults to the ranges of the benchmark configuration
+    (viscosity ratio 2..20, porosity 0.6..0.85, inlet 0.005..0.02).  Family
+    "stable" defaults to viscosity ratio 2..5, porosity 0.70..0.85 and inlet
+    0.003..0.010: with the reference's velocity inlet and velocity outlet the
+    medium must carry the imposed flux with density differences of order
+    3 u nu L / k (Darcy), and denser or faster members crash (rho -> 0 at the
+    outlet) within a few thousand steps; on the 96-member draw of seed 2024
+    none of these diverges within 6000 steps, against 35 of 96 with the
+    configuration's porosity and inlet ranges."""
     if ratio is None:
         ratio = (2.0, 20.0) if family == "spec" else (2.0, 5.0)
+    if porosity is None:
+        porosity = (0.6, 0.85) if family == "spec" else (0.70, 0.85)
+    if u_in is None:
+        u_in = (0.005, 0.02) if family == "spec" else (0.003, 0.010)
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
