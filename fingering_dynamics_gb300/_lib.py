@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(PKG, "_lib", "libfdlbm.so")
 FD_OK = 0
 FD_F64, FD_F32, FD_F16, FD_BF16 = 0, 1, 2, 3
 FD_VARIANT_PERIODIC, FD_VARIANT_WALLS = 0, 1
-FD_INIT_MU, FD_INIT_UY = 1, 2
+FD_INIT_MU, FD_INIT_UY, FD_INIT_VELOCITY = 1, 2, 4
 FD_ROUND_NEAREST, FD_ROUND_STOCHASTIC = 0, 1
 ROUNDING = {"nearest": FD_ROUND_NEAREST, "stochastic": FD_ROUND_STOCHASTIC}
 TERMS = {"large_F": 0, "feq": 1, "geq": 2, "F": 3, "G": 4}
@@ -61,7 +61,7 @@ class fd_fields(C.Structure):
                                           "mix_tau")]
 
 
-_VP, _I, _PD = C.c_void_p, C.c_int, C.c_ssize_t
+_VP, _I, _PD, _SZ, _FL = C.c_void_p, C.c_int, C.c_ssize_t, C.c_size_t, C.c_float
 _P = C.POINTER(fd_params)
 _S = C.POINTER(fd_storage)
 _F = C.POINTER(fd_fields)
@@ -97,8 +97,27 @@ SIGNATURES = {
     "fd_batch_tiles": [_VP],
     "fd_batch_destroy": [_VP],
     "fd_diagnostics": [_P, _I, _S, _VP, _VP, _VP, _VP, _VP],
+    # learned surrogate (include/fdsurrogate.h)
+    "sg_conv3x3": [_VP, _I, _I, _I, _I, _VP, _VP, _I, _I, _VP, _VP, _VP],
+    "sg_flip_weights": [_VP, _I, _I, _VP, _VP],
+    "sg_conv3x3_wgrad": [_VP, _VP, _I, _I, _I, _I, _I, _VP, _VP, _SZ, _I, _VP],
+    "sg_wgrad_partial_floats": [_I, _I, _I, _I, _I],
+    "sg_bias_grad": [_VP, _SZ, _I, _VP, _VP, _VP],
+    "sg_bias_partial_floats": [_I],
+    "sg_gelu_bwd": [_VP, _VP, _SZ, _VP, _VP],
+    "sg_pool2": [_VP, _I, _I, _I, _I, _VP, _VP],
+    "sg_pool2_bwd": [_VP, _I, _I, _I, _I, _VP, _VP],
+    "sg_up2": [_VP, _I, _I, _I, _I, _VP, _I, _I, _VP],
+    "sg_up2_bwd": [_VP, _I, _I, _I, _I, _I, _I, _VP, _VP],
+    "sg_copy_channels": [_VP, _SZ, _I, _VP, _I, _I, _VP],
+    "sg_add_channels": [_VP, _SZ, _I, _I, _I, _VP, _VP],
+    "sg_masked_mse": [_VP, _VP, _VP, _SZ, _I, _VP, _VP, _FL, _VP],
+    "sg_loss_blocks": [],
+    "sg_adamw": [_VP, _VP, _VP, _VP, _VP, _SZ, _FL, _FL, _FL, _FL, _FL, _I, _VP],
+    "sg_to_bf16": [_VP, _SZ, _VP, _VP],
 }
-_RET = {"fd_last_error": C.c_char_p, "fd_packed_bytes": C.c_size_t, "fd_diag_scratch_bytes": C.c_size_t}
+_RET = {"fd_last_error": C.c_char_p, "fd_packed_bytes": C.c_size_t, "fd_diag_scratch_bytes": C.c_size_t,
+        "sg_wgrad_partial_floats": C.c_size_t, "sg_bias_partial_floats": C.c_size_t}
 
 _lock = threading.Lock()
 _handle = None

@@ -37,6 +37,7 @@ UNITS = {
     "fd_noalloc.cu": [],
     "fd_diag.cu": [],
     "fd_batch.cu": [],
+    "sg_kernels.cu": [],
 }
 
 

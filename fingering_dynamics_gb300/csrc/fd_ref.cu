@@ -103,8 +103,13 @@ __global__ void k_init_rest(Shape s, Coef<T> c, unsigned flags, const uint16_t* 
   m.gx = gx; m.gy = gy;
   m.p = pressure_of(c, m.rho, m.psi, T(0));                  // getP with mu = 0 (fingering_periodic.py:111,117)
   m.mu = (flags & FD_INIT_MU) ? chem_pot(c, m.psi, lap) : T(0);               // fingering.py:122
-  m.ux = T(0);
-  m.uy = (flags & FD_INIT_UY) ? velocity_of(T(0), m.mu, gy, m.rho) : T(0);    // fingering.py:123
+  if (flags & FD_INIT_VELOCITY) {  // caller-supplied u (no reference counterpart: the scripts start at rest)
+    m.ux = F.ux[q];
+    m.uy = F.uy[q];
+  } else {
+    m.ux = T(0);
+    m.uy = (flags & FD_INIT_UY) ? velocity_of(T(0), m.mu, gy, m.rho) : T(0);  // fingering.py:123
+  }
   m.tau_mix = mix_tau_of(c, m.rho, m.psi);
   F.ux[q] = m.ux; F.uy[q] = m.uy; F.p[q] = m.p; F.mu[q] = m.mu; F.mix_tau[q] = m.tau_mix;
   const CollisionTerms<T> t = collision_terms(c, m);

@@ -213,6 +213,40 @@ class Lattice:
             self.scur = 1 - self.scur
         self.iteration += n
 
+    def peek(self):
+        """Fields of the next iteration (psi, rho, ux, uy, ... in the field
+        tensors) without leaving fused mode: the pending packed state is
+        unpacked into the reference-layout buffers, which the fused state does
+        not use, and finished there.  The state itself is not touched, so a
+        lattice that is a member of an ensemble can be read between batched
+        steps."""
+        self._require("fused")
+        if self.storage is None:
+            raise ValueError("peek needs packed storage (dtype f32, f16 or bf16)")
+        L.call("fd_unpack", C.byref(self.prm), C.byref(self.storage), _ptr(self.ppop[self.pcur]), self.fd_dtype,
+               _ptr(self.pop[self.cur]), self._stream())
+        self._finish_from(self.pop[self.cur], self.side[self.scur], self.pop[1 - self.cur])
+
+    def restart_from_fields(self, psi, ux, uy, rho=None, iteration: int | None = None):
+        """Replace the state by the equilibrium of the given fields ((H, W)
+        device tensors or arrays): populations f = feq(rho, u, psi, mu(psi)),
+        g = geq, as Compute.__init__ builds them (fingering_periodic.py:
+        100-121) but with the given velocity (FD_INIT_VELOCITY).  Leaves the
+        lattice in reference mode at ``iteration`` (default: unchanged)."""
+        dev, td = self.device, self.tdtype
+        self.mode = "reference"
+        self.ux.copy_(torch.as_tensor(ux, device=dev, dtype=td))
+        self.uy.copy_(torch.as_tensor(uy, device=dev, dtype=td))
+        psi_d = torch.as_tensor(psi, device=dev).to(torch.float64).contiguous()
+        rho_d = None if rho is None else torch.as_tensor(rho, device=dev).to(torch.float64).contiguous()
+        prm = L.fd_params.from_buffer_copy(self.prm)
+        prm.flags |= L.FD_INIT_MU | L.FD_INIT_VELOCITY
+        L.call("fd_compute_init", C.byref(prm), self.fd_dtype, _ptr(self.mask), _ptr(psi_d), _ptr(rho_d),
+               C.byref(self.fields()), self._stream())
+        torch.cuda.current_stream(self.device).synchronize()
+        if iteration is not None:
+            self.iteration = int(iteration)
+
     def step_seed(self) -> int:
         """Stochastic-rounding seed of the next fused launch."""
         return (self.seed + self.iteration) & 0xFFFFFFFF

@@ -1,0 +1,415 @@
+"""Learned surrogate: a convolutional U-Net that advances (psi, u_x, u_y) by a
+fixed number of lattice steps (a "jump") given the solid mask, trained on
+trajectories of the batched LBM with this package's own CUDA kernels
+(include/fdsurrogate.h: tensor-core implicit-GEMM convolutions forward, data
+and weight gradients, and the training elementwise kernels), and a rollout
+driver that uses the plain LBM as its judge and fallback.
+
+The reference has no learned component.  Network (widths c1..c4, 3x3 convs,
+GELU, 2x2 mean pooling, nearest upsampling, skip concatenation):
+
+    e1 = G(conv(G(conv(x, c1)), c1))                       H x W
+    e2 = G(conv(G(conv(pool(e1), c2)), c2))                H/2
+    e3 = G(conv(G(conv(pool(e2), c3)), c3))                H/4
+    e4 = G(conv(G(conv(pool(e3), c4)), c4))                H/8
+    d3 = G(conv(G(conv([up(e4), e3], c3)), c3))            H/4
+    d2 = G(conv(G(conv([up(d3), e2], c2)), c2))            H/2
+    d1 = G(conv(G(conv([up(d2), e1], c1)), c1))            H x W
+    out = conv(d1, 16);  prediction = x[..., :3] + out[..., :3]
+
+A frame is NHWC bfloat16 with 16 channels: psi, u_x / U, u_y / U, solid (1 on
+solid cells), zeros; U = ``VELOCITY_SCALE``.  The output layer starts at
+zero, so the untrained network predicts "no change" (persistence).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+VELOCITY_SCALE = 0.01
+FRAME_CHANNELS = 16
+LAYERS = ("enc1a", "enc1b", "enc2a", "enc2b", "enc3a", "enc3b", "enc4a", "enc4b",
+          "dec3a", "dec3b", "dec2a", "dec2b", "dec1a", "dec1b", "out")
+
+
+def layer_shapes(c=(32, 64, 128, 256), cin=FRAME_CHANNELS, cout=FRAME_CHANNELS):
+    c1, c2, c3, c4 = c
+    return {"enc1a": (cin, c1), "enc1b": (c1, c1), "enc2a": (c1, c2), "enc2b": (c2, c2),
+            "enc3a": (c2, c3), "enc3b": (c3, c3), "enc4a": (c3, c4), "enc4b": (c4, c4),
+            "dec3a": (c4 + c3, c3), "dec3b": (c3, c3), "dec2a": (c3 + c2, c2), "dec2b": (c2, c2),
+            "dec1a": (c2 + c1, c1), "dec1b": (c1, c1), "out": (c1, cout)}
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _s():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def frame_from_fields(psi, ux, uy, solid) -> torch.Tensor:
+    """(H, W) device tensors -> one frame (H, W, 16) bfloat16."""
+    H, W = psi.shape
+    fr = torch.zeros((H, W, FRAME_CHANNELS), dtype=torch.float32, device=psi.device)
+    fl = ~solid
+    fr[..., 0] = psi.float()
+    fr[..., 1] = torch.where(fl, ux.float(), 0) / VELOCITY_SCALE
+    fr[..., 2] = torch.where(fl, uy.float(), 0) / VELOCITY_SCALE
+    fr[..., 3] = solid.float()
+    return fr.to(torch.bfloat16)
+
+
+def fields_from_frame(fr: torch.Tensor):
+    """One frame -> (psi, ux, uy) float32 (H, W) tensors."""
+    f = fr.float()
+    return f[..., 0], f[..., 1] * VELOCITY_SCALE, f[..., 2] * VELOCITY_SCALE
+
+
+class UNet:
+    """The network, its FP32 master weights, bfloat16 copies, AdamW moments and
+    activation buffers (allocated per batch shape)."""
+
+    def __init__(self, widths=(32, 64, 128, 256), seed: int = 0, device="cuda", params: dict | None = None):
+        self.widths = tuple(widths)
+        self.shapes = layer_shapes(self.widths)
+        self.device = torch.device(device)
+        rng = np.random.default_rng(seed)
+        self.w, self.b = {}, {}
+        for name, (ci, co) in self.shapes.items():
+            if params is not None:
+                w = np.asarray(params[name + ".w"], np.float32)
+                b = np.asarray(params[name + ".b"], np.float32)
+            else:
+                std = math.sqrt(2.0 / (9 * ci))
+                w = (rng.normal(0.0, std, (co, 3, 3, ci)) * (0.0 if name == "out" else 1.0)).astype(np.float32)
+                b = np.zeros(co, np.float32)
+            self.w[name] = torch.from_numpy(w).to(self.device).contiguous()
+            self.b[name] = torch.from_numpy(b).to(self.device).contiguous()
+        self.w16 = {n: t.to(torch.bfloat16) for n, t in self.w.items()}
+        self.wt16 = {n: torch.empty((ci, 3, 3, co), dtype=torch.bfloat16, device=self.device)
+                     for n, (ci, co) in self.shapes.items()}
+        self.gw = {n: torch.zeros_like(t) for n, t in self.w.items()}
+        self.gb = {n: torch.zeros_like(t) for n, t in self.b.items()}
+        self.mw = {n: torch.zeros_like(t) for n, t in self.w.items()}
+        self.vw = {n: torch.zeros_like(t) for n, t in self.w.items()}
+        self.mb = {n: torch.zeros_like(t) for n, t in self.b.items()}
+        self.vb = {n: torch.zeros_like(t) for n, t in self.b.items()}
+        self.steps = 0
+        self._buf = {}
+        self._flipped = False
+
+    @property
+    def n_params(self) -> int:
+        return sum(t.numel() for t in self.w.values()) + sum(t.numel() for t in self.b.values())
+
+    def flops_forward(self, N, H, W) -> float:
+        """Multiply-adds x 2 of the convolutions of one forward pass."""
+        f, lvl = 0.0, {"1": 1, "2": 2, "3": 4, "4": 8}
+        for name, (ci, co) in self.shapes.items():
+            d = 1 if name == "out" else lvl[name[3]]
+            f += 2.0 * 9 * ci * co * N * (H // d) * (W // d)
+        return f
+
+    def state_dict(self) -> dict:
+        out = {}
+        for n in LAYERS:
+            out[n + ".w"] = self.w[n].cpu().numpy()
+            out[n + ".b"] = self.b[n].cpu().numpy()
+        return out
+
+    # ------------------------------------------------------------------
+    def _buffers(self, N, H, W):
+        key = (N, H, W)
+        if key in self._buf:
+            return self._buf[key]
+        if H % 8 or W % 8:
+            raise ValueError("frame height and width must be multiples of 8")
+        c1, c2, c3, c4 = self.widths
+        dev, bf = self.device, torch.bfloat16
+        lv = {1: (H, W), 2: (H // 2, W // 2), 3: (H // 4, W // 4), 4: (H // 8, W // 8)}
+
+        def t(level, ch):
+            h, w = lv[level]
+            return torch.empty((N, h, w, ch), dtype=bf, device=dev)
+
+        level = {"enc1a": 1, "enc1b": 1, "enc2a": 2, "enc2b": 2, "enc3a": 3, "enc3b": 3, "enc4a": 4, "enc4b": 4,
+                 "dec3a": 3, "dec3b": 3, "dec2a": 2, "dec2b": 2, "dec1a": 1, "dec1b": 1, "out": 1}
+        B = {"level": level, "lv": lv}
+        for name, (ci, co) in self.shapes.items():
+            B["z." + name] = t(level[name], co)
+            B["y." + name] = t(level[name], co)
+            B["dy." + name] = t(level[name], co)
+            B["dz." + name] = t(level[name], co)
+            B["dx." + name] = t(level[name], ci)
+        B["p1"], B["p2"], B["p3"] = t(2, c1), t(3, c2), t(4, c3)
+        B["u3"], B["u2"], B["u1"] = t(3, c4 + c3), t(2, c3 + c2), t(1, c2 + c1)
+        B["de1"], B["de2"], B["de3"] = t(1, c1), t(2, c2), t(3, c3)
+        wp = max(L.lib().sg_wgrad_partial_floats(N, *lv[level[n]], ci, co) for n, (ci, co) in self.shapes.items())
+        B["wpart"] = torch.empty(int(wp), dtype=torch.float32, device=dev)
+        B["bpart"] = torch.empty(int(L.lib().sg_bias_partial_floats(max(c1, c2, c3, c4, FRAME_CHANNELS))),
+                                 dtype=torch.float32, device=dev)
+        B["lpart"] = torch.empty(2 * L.lib().sg_loss_blocks(), dtype=torch.float32, device=dev)
+        self._buf[key] = B
+        return B
+
+    def _conv(self, name, x, B, act=True):
+        ci, co = self.shapes[name]
+        N, h, w, c = x.shape
+        assert c == ci, (name, c, ci)
+        L.call("sg_conv3x3", _p(x), N, h, w, ci, _p(self.w16[name]), _p(self.b[name]), co,
+               1 if act else 0, _p(B["z." + name]) if act else None, _p(B["y." + name]), _s())
+        return B["y." + name]
+
+    def forward(self, x: torch.Tensor) -> torch.Tensor:
+        """x: (N, H, W, 16) bfloat16 frames -> out (N, H, W, 16) bfloat16 (the
+        prediction is x[..., :3] + out[..., :3])."""
+        N, H, W, _ = x.shape
+        B = self._buffers(N, H, W)
+        c1, c2, c3, c4 = self.widths
+        lv = B["lv"]
+        s = _s()
+        self._x = x
+        e1 = self._conv("enc1b", self._conv("enc1a", x, B), B)
+        L.call("sg_pool2", _p(e1), N, H, W, c1, _p(B["p1"]), s)
+        e2 = self._conv("enc2b", self._conv("enc2a", B["p1"], B), B)
+        L.call("sg_pool2", _p(e2), N, *lv[2], c2, _p(B["p2"]), s)
+        e3 = self._conv("enc3b", self._conv("enc3a", B["p2"], B), B)
+        L.call("sg_pool2", _p(e3), N, *lv[3], c3, _p(B["p3"]), s)
+        e4 = self._conv("enc4b", self._conv("enc4a", B["p3"], B), B)
+        L.call("sg_up2", _p(e4), N, *lv[4], c4, _p(B["u3"]), c4 + c3, 0, s)
+        L.call("sg_copy_channels", _p(e3), N * lv[3][0] * lv[3][1], c3, _p(B["u3"]), c4 + c3, c4, s)
+        d3 = self._conv("dec3b", self._conv("dec3a", B["u3"], B), B)
+        L.call("sg_up2", _p(d3), N, *lv[3], c3, _p(B["u2"]), c3 + c2, 0, s)
+        L.call("sg_copy_channels", _p(e2), N * lv[2][0] * lv[2][1], c2, _p(B["u2"]), c3 + c2, c3, s)
+        d2 = self._conv("dec2b", self._conv("dec2a", B["u2"], B), B)
+        L.call("sg_up2", _p(d2), N, *lv[2], c2, _p(B["u1"]), c2 + c1, 0, s)
+        L.call("sg_copy_channels", _p(e1), N * H * W, c1, _p(B["u1"]), c2 + c1, c2, s)
+        d1 = self._conv("dec1b", self._conv("dec1a", B["u1"], B), B)
+        return self._conv("out", d1, B, act=False)
+
+    def predict(self, x: torch.Tensor) -> torch.Tensor:
+        """Frames one jump later: x[..., :3] + out[..., :3], other channels of x."""
+        out = self.forward(x)
+        y = x.clone()
+        y[..., :3] = (x[..., :3].float() + out[..., :3].float()).to(torch.bfloat16)
+        return y
+
+    # ------------------------------------------------------------------
+    def _flip_all(self):
+        s = _s()
+        for name, (ci, co) in self.shapes.items():
+            L.call("sg_flip_weights", _p(self.w16[name]), ci, co, _p(self.wt16[name]), s)
+        self._flipped = True
+
+    def _layer_back(self, name, inp, dz, B, need_dx=True):
+        """Weight / bias gradients of layer `name` from dz; returns dx."""
+        ci, co = self.shapes[name]
+        N, h, w, _ = inp.shape
+        s = _s()
+        L.call("sg_conv3x3_wgrad", _p(inp), _p(dz), N, h, w, ci, co, _p(self.gw[name]), _p(B["wpart"]),
+               B["wpart"].numel(), 0, s)
+        L.call("sg_bias_grad", _p(dz), N * h * w, co, _p(self.gb[name]), _p(B["bpart"]), s)
+        if not need_dx:
+            return None
+        dx = B["dx." + name]
+        L.call("sg_conv3x3", _p(dz), N, h, w, co, _p(self.wt16[name]), None, ci, 0, None, _p(dx), s)
+        return dx
+
+    def _gelu_back(self, name, dy, B):
+        dz = B["dz." + name]
+        L.call("sg_gelu_bwd", _p(dy), _p(B["z." + name]), dy.numel(), _p(dz), _s())
+        return dz
+
+    def _block_back(self, name, inp, dy, B, need_dx=True):
+        return self._layer_back(name, inp, self._gelu_back(name, dy, B), B, need_dx)
+
+    def backward(self, dout: torch.Tensor):
+        """Gradients (self.gw, self.gb) of the loss whose gradient w.r.t. the
+        output of the last forward() is dout."""
+        if not self._flipped:
+            self._flip_all()
+        x = self._x
+        N, H, W, _ = x.shape
+        B = self._buffers(N, H, W)
+        lv = B["lv"]
+        c1, c2, c3, c4 = self.widths
+        s = _s()
+        y = lambda n: B["y." + n]
+        dd1 = self._layer_back("out", y("dec1b"), dout, B)
+        du1 = self._block_back("dec1a", B["u1"], self._block_back("dec1b", y("dec1a"), dd1, B), B)
+        dd2 = B["dy.dec2b"]
+        L.call("sg_up2_bwd", _p(du1), N, *lv[2], c2 + c1, 0, c2, _p(dd2), s)
+        du2 = self._block_back("dec2a", B["u2"], self._block_back("dec2b", y("dec2a"), dd2, B), B)
+        dd3 = B["dy.dec3b"]
+        L.call("sg_up2_bwd", _p(du2), N, *lv[3], c3 + c2, 0, c3, _p(dd3), s)
+        du3 = self._block_back("dec3a", B["u3"], self._block_back("dec3b", y("dec3a"), dd3, B), B)
+        de4 = B["dy.enc4b"]
+        L.call("sg_up2_bwd", _p(du3), N, *lv[4], c4 + c3, 0, c4, _p(de4), s)
+        dp3 = self._block_back("enc4a", B["p3"], self._block_back("enc4b", y("enc4a"), de4, B), B)
+        de3 = B["de3"]
+        L.call("sg_pool2_bwd", _p(dp3), N, *lv[3], c3, _p(de3), s)
+        L.call("sg_add_channels", _p(du3), N * lv[3][0] * lv[3][1], c4 + c3, c4, c3, _p(de3), s)
+        dp2 = self._block_back("enc3a", B["p2"], self._block_back("enc3b", y("enc3a"), de3, B), B)
+        de2 = B["de2"]
+        L.call("sg_pool2_bwd", _p(dp2), N, *lv[2], c2, _p(de2), s)
+        L.call("sg_add_channels", _p(du2), N * lv[2][0] * lv[2][1], c3 + c2, c3, c2, _p(de2), s)
+        dp1 = self._block_back("enc2a", B["p1"], self._block_back("enc2b", y("enc2a"), de2, B), B)
+        de1 = B["de1"]
+        L.call("sg_pool2_bwd", _p(dp1), N, H, W, c1, _p(de1), s)
+        L.call("sg_add_channels", _p(du1), N * H * W, c2 + c1, c2, c1, _p(de1), s)
+        self._block_back("enc1a", x, self._block_back("enc1b", y("enc1a"), de1, B), B, need_dx=False)
+
+    def loss_grad(self, x: torch.Tensor, xn: torch.Tensor) -> torch.Tensor:
+        """Forward, masked MSE of the prediction against xn, backward.
+        Returns the loss as a 0-d device tensor (no host sync)."""
+        N, H, W, Cc = x.shape
+        out = self.forward(x)
+        B = self._buffers(N, H, W)
+        count = max(float((x[..., 3] == 0).sum().item()), 1.0)
+        dout = B["dy.out"]
+        L.call("sg_masked_mse", _p(x), _p(out), _p(xn), N * H * W, Cc, _p(dout), _p(B["lpart"]),
+               C.c_float(1.0 / (3.0 * count)), _s())
+        self.backward(dout)
+        lp = B["lpart"].view(-1, 2)
+        return lp[:, 0].sum() / (3.0 * count)
+
+    def adamw(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=1e-2):
+        self.steps += 1
+        s = _s()
+        for n in LAYERS:
+            L.call("sg_adamw", _p(self.w[n]), _p(self.w16[n]), _p(self.gw[n]), _p(self.mw[n]), _p(self.vw[n]),
+                   self.w[n].numel(), lr, beta1, beta2, eps, weight_decay, self.steps, s)
+            L.call("sg_adamw", _p(self.b[n]), None, _p(self.gb[n]), _p(self.mb[n]), _p(self.vb[n]),
+                   self.b[n].numel(), lr, beta1, beta2, eps, 0.0, self.steps, s)
+        self._flipped = False
+
+
+# ----------------------------------------------------------------------------
+# data: trajectories of the batched LBM
+# ----------------------------------------------------------------------------
+def member_frame(lat) -> torch.Tensor:
+    """Frame of the next iteration of a fused-mode lattice (Lattice.peek)."""
+    lat.peek()
+    return frame_from_fields(lat.psi, lat.ux, lat.uy, ~lat.fluid)
+
+
+def generate_trajectories(specs, n_frames: int, jump: int = 200, dtype: str = "f32", warmup: int = 0):
+    """Advance an ensemble of members (MemberSpec) with the batched LBM and
+    record a frame of every member every `jump` iterations.  Returns frames
+    (members, n_frames, H, W, 16) bfloat16 on the GPU (all members must share
+    one lattice size) and the ensemble's finite flags."""
+    from .ensemble import Ensemble
+    ens = Ensemble([s.build() for s in specs], dtype=dtype)
+    if warmup:
+        ens.step(warmup)
+    H, W = ens.lattices[0].H, ens.lattices[0].W
+    frames = torch.empty((len(specs), n_frames, H, W, FRAME_CHANNELS), dtype=torch.bfloat16,
+                         device=ens.lattices[0].device)
+    for k in range(n_frames):
+        if k:
+            ens.step(jump)
+        torch.cuda.current_stream().wait_stream(ens.stream)
+        for m, lat in enumerate(ens.lattices):
+            frames[m, k] = member_frame(lat)
+    finite = torch.isfinite(frames.float().view(len(specs), -1)).all(dim=1)
+    ens.close()
+    return frames, finite
+
+
+def train(net: UNet, frames: torch.Tensor, steps: int, batch: int = 32, lr: float = 1e-3, seed: int = 0,
+          log_every: int = 0):
+    """AdamW on random (frame k, frame k+1) pairs of `frames`
+    (members, n_frames, H, W, 16).  Returns the loss history (host floats)."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    M, F = frames.shape[:2]
+    hist = []
+    for it in range(steps):
+        mi = torch.randint(0, M, (batch,), generator=g)
+        fi = torch.randint(0, F - 1, (batch,), generator=g)
+        x = frames[mi, fi].contiguous()
+        xn = frames[mi, fi + 1].contiguous()
+        loss = net.loss_grad(x, xn)
+        net.adamw(lr=lr)
+        if log_every and (it % log_every == 0 or it == steps - 1):
+            hist.append((it, float(loss.item())))
+    return hist
+
+
+def evaluate(net: UNet, frames: torch.Tensor, batch: int = 16) -> dict:
+    """Masked MSE of the network and of persistence (no change) over every
+    consecutive pair of `frames`."""
+    M, F = frames.shape[:2]
+    se_net = se_per = cnt = 0.0
+    pairs = [(m, k) for m in range(M) for k in range(F - 1)]
+    for i in range(0, len(pairs), batch):
+        mi = torch.tensor([p[0] for p in pairs[i:i + batch]])
+        fi = torch.tensor([p[1] for p in pairs[i:i + batch]])
+        x = frames[mi, fi].contiguous()
+        xn = frames[mi, fi + 1].contiguous()
+        pred = net.predict(x).float()[..., :3]
+        tgt = xn.float()[..., :3]
+        fl = (x[..., 3] == 0).unsqueeze(-1).float()
+        se_net += float((((pred - tgt) ** 2) * fl).sum())
+        se_per += float((((x.float()[..., :3] - tgt) ** 2) * fl).sum())
+        cnt += float(fl.sum()) * 3
+    return {"mse_net": se_net / cnt, "mse_persistence": se_per / cnt, "gain": se_per / max(se_net, 1e-30)}
+
+
+# ----------------------------------------------------------------------------
+# rollout with the LBM as judge
+# ----------------------------------------------------------------------------
+def saturation(psi, fluid) -> float:
+    return float(((psi > 0) & fluid).sum().item() / max(int(fluid.sum().item()), 1))
+
+
+def rollout(net: UNet, lat, jumps_per_check: int = 5, checks: int = 4, jump: int = 200, tol: float = 0.02):
+    """Advance a reference-mode Lattice by surrogate jumps, judged by the LBM.
+
+    Each round: `jumps_per_check` surrogate jumps from the current state, the
+    lattice restarted from the equilibrium of the predicted fields (density
+    kept from the last LBM state), then `jump` LBM iterations as the judge.
+    The round is accepted if the judged saturation is within `tol` (relative)
+    of the surrogate's prediction for the same iteration (one more jump);
+    otherwise the lattice falls back to plain LBM from the round's start.
+    Returns per-round records and timings."""
+    fluid = lat.fluid
+    solid = ~fluid
+    records = []
+    for r in range(checks):
+        start_it = lat.iteration
+        t0 = time.perf_counter()
+        saved = {k: getattr(lat, k).clone() for k in ("psi", "ux", "uy", "rho")}
+        x = frame_from_fields(lat.psi, lat.ux, lat.uy, solid).unsqueeze(0).contiguous()
+        for _ in range(jumps_per_check):
+            x = net.predict(x)
+        psi, ux, uy = fields_from_frame(x[0])
+        nxt = net.predict(x)
+        psi_next, _, _ = fields_from_frame(nxt[0])
+        torch.cuda.synchronize()
+        t_sur = time.perf_counter() - t0
+        lat.restart_from_fields(torch.where(fluid, psi, lat.params.psi_wall), ux, uy, rho=lat.rho,
+                                iteration=start_it + jumps_per_check * jump)
+        t1 = time.perf_counter()
+        lat.step(jump)
+        torch.cuda.synchronize()
+        t_judge = time.perf_counter() - t1
+        s_lbm = saturation(lat.psi, fluid)
+        s_sur = saturation(psi_next, fluid)
+        ok = bool(np.isfinite(s_lbm)) and abs(s_lbm - s_sur) <= tol * max(s_lbm, 1e-12)
+        rec = {"round": r, "start": start_it, "accepted": ok, "sat_lbm": s_lbm, "sat_surrogate": s_sur,
+               "t_surrogate_s": t_sur, "t_judge_s": t_judge}
+        if not ok:  # fall back: plain LBM from the round's start
+            lat.restart_from_fields(saved["psi"], saved["ux"], saved["uy"], rho=saved["rho"], iteration=start_it)
+            t2 = time.perf_counter()
+            lat.step((jumps_per_check + 1) * jump)
+            torch.cuda.synchronize()
+            rec["t_fallback_s"] = time.perf_counter() - t2
+        records.append(rec)
+    return records

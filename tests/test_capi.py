@@ -1,5 +1,6 @@
-"""The C-ABI library builds, loads and exports every symbol include/fdlbm.h
-declares (no GPU needed: nothing is launched)."""
+"""The C-ABI library builds, loads and exports every symbol include/*.h
+declares, and the ctypes table binds exactly those (no GPU needed: nothing is
+launched)."""
 import ctypes
 import os
 import re
@@ -15,7 +16,7 @@ def declared_functions():
         if fn.endswith(".h"):
             src = open(os.path.join(REPO, "include", fn)).read()
             src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(fd_\w+)\s*\(", src, flags=re.M)
+            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*((?:fd|sg)_\w+)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 
@@ -35,6 +36,12 @@ def test_header_declares_entry_points():
 def test_every_declared_symbol_is_exported(lib):
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_binding_table_matches_headers():
+    from fingering_dynamics_gb300 import _lib as L
+    assert sorted(L.SIGNATURES) == declared_functions()
+    assert any(n.startswith("sg_") for n in L.SIGNATURES)
 
 
 def test_abi_version_and_error_path(lib):
