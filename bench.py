@@ -385,6 +385,89 @@ def run_precision(args):
     return 0
 
 
+def run_surrogate(args):
+    """BASELINE configs[4]: the learned surrogate at 512 x 256.  Trajectories of
+    a seeded ensemble (batched LBM, one frame every 200 iterations), the last
+    10% of geometries held out; AdamW training of the U-Net (32/64/128/256)
+    with the project's tensor-core kernels, timed with CUDA events; held-out
+    error against persistence, autoregressive saturation error, and the time
+    of one jump against 200 batched LBM iterations of the same members."""
+    import torch
+    from fingering_dynamics_gb300 import build
+    from fingering_dynamics_gb300.ensemble import Ensemble, ensemble_specs
+    from fingering_dynamics_gb300.surrogate import (UNet, evaluate, expand, generate_trajectories,
+                                                    rollout_saturation_error, train)
+    build.build()
+    H, W, jump = 256, 512, 200
+    M = args.members
+    specs = ensemble_specs(M, seed=2024, sizes_w=(W,), sizes_h=(H,))
+    held = max(1, M // 10)
+    t0 = time.perf_counter()
+    frames, finite = generate_trajectories(specs, n_frames=args.frames, jump=jump)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    fin = finite.cpu().numpy()
+    train_idx = [i for i in range(M - held) if fin[i]]
+    test_idx = [i for i in range(M - held, M) if fin[i]]
+    train_f, test_f = frames[train_idx], frames[test_idx]
+    net = UNet((32, 64, 128, 256), seed=0)
+    train(net, train_f, steps=args.warmup, batch=args.batch, seed=1)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        hist = train(net, train_f, steps=args.train_steps, batch=args.batch, lr=1e-3, seed=2,
+                     log_every=max(1, args.train_steps // 10))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms_step = e0.elapsed_time(e1) / args.train_steps
+    flops_step = 3.0 * net.flops_forward(args.batch, H, W)
+    tflops = flops_step / (ms_step / 1e3) / 1e12
+    ev = evaluate(net, test_f)
+    roll = rollout_saturation_error(net, test_f, start=0, jumps=5)
+    # one jump of `batch` members: surrogate forward vs 200 batched LBM iterations
+    nb = min(args.batch, M)
+    ens = Ensemble([s.build() for s in specs[:nb]])
+    ens.step(5)
+    t_lbm = ens.time_steps(jump, use_graph=True)
+    ens.close()
+    x = expand(frames[:nb, 0])
+    for _ in range(3):
+        net.forward(x)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(10):
+        net.forward(x)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t_sur = f0.elapsed_time(f1) / 10 / 1e3
+    peak = None
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        peak = float(json.load(open(p))["bf16_tflops_sustained"])
+    peak_kind = "measured (sustained)" if peak else "fallback"
+    peak = peak or 1700.0
+    line = {"metric": "surrogate training throughput (tensor-core convolutions, fwd + data + weight gradients)",
+            "value": round(tflops, 2), "unit": "TFLOP/s", "higher_is_better": True, "n_gpus": 1,
+            "steps": args.train_steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "dtype": "bf16",
+            "data": "synthetic (batched-LBM trajectories)",
+            "config": {"workload": f"unet_{W}x{H}_batch{args.batch}", "widths": [32, 64, 128, 256],
+                       "params": net.n_params, "members": M, "held_out_members": len(test_idx),
+                       "train_members": len(train_idx), "frames_per_member": args.frames, "jump": jump,
+                       "train_pairs": len(train_idx) * (args.frames - 1),
+                       "flops_per_step": flops_step, "data_generation_s": round(t_data, 1)},
+            "roofline": {"bound": "tensor", "achieved": round(tflops, 2), "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(tflops / peak, 4), "peak_kind": peak_kind, "traffic": None},
+            "loss_history": hist, "held_out": ev, "rollout_saturation_rel_error": roll,
+            "jump_vs_lbm": {"members": nb, "lbm_200_iterations_ms": round(t_lbm * 1e3, 3),
+                            "surrogate_jump_ms": round(t_sur * 1e3, 3), "speedup": round(t_lbm / t_sur, 2),
+                            "speedup_with_judge": round(6 * t_lbm / (6 * t_sur + t_lbm), 2)},
+            "gpu_launches": None, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -397,14 +480,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end measurement")
     ap.add_argument("--H", type=int, default=H_FULL, help="lattice rows (default: the 4096 x 2048 workload)")
     ap.add_argument("--W", type=int, default=W_FULL, help="lattice columns")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "precision"],
+    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "precision", "surrogate"],
                     help="single 4096 x 2048 lattice (default), the batched ensemble, or the error study of "
                          "reduced-precision storage against the FP64 path (1024 x 256, --steps iterations)")
     ap.add_argument("--rounding", default="stochastic", choices=["stochastic", "nearest"],
                     help="rounding of FP16/BF16 population stores")
     ap.add_argument("--every", type=int, default=500, help="precision study: iterations between comparisons")
     ap.add_argument("--out", default=None, help="precision study: write the full curves to this JSON file")
-    ap.add_argument("--members", type=int, default=96, help="ensemble members")
+    ap.add_argument("--members", type=int, default=96, help="ensemble members (surrogate: trajectory members)")
+    ap.add_argument("--frames", type=int, default=41, help="surrogate: frames per member (one per 200 iterations)")
+    ap.add_argument("--train-steps", type=int, default=1000, help="surrogate: timed AdamW steps")
+    ap.add_argument("--batch", type=int, default=32, help="surrogate: training batch")
     ap.add_argument("--family", default="stable", choices=["stable", "spec"],
                     help="ensemble parameter family (spec: the configuration's literal ranges)")
     args = ap.parse_args()
@@ -416,6 +502,8 @@ def main():
         return run_ensemble(args)
     if args.workload == "precision":
         return run_precision(args)
+    if args.workload == "surrogate":
+        return run_surrogate(args)
     return run_ours(args)
 
 

@@ -66,6 +66,11 @@ def frame_from_fields(psi, ux, uy, solid) -> torch.Tensor:
     return fr.to(torch.bfloat16)
 
 
+def expand(frames4: torch.Tensor) -> torch.Tensor:
+    """Frames stored with their 4 live channels -> the network's 16 channels."""
+    return torch.nn.functional.pad(frames4, (0, FRAME_CHANNELS - frames4.shape[-1])).contiguous()
+
+
 def fields_from_frame(fr: torch.Tensor):
     """One frame -> (psi, ux, uy) float32 (H, W) tensors."""
     f = fr.float()
@@ -303,21 +308,21 @@ def member_frame(lat) -> torch.Tensor:
 def generate_trajectories(specs, n_frames: int, jump: int = 200, dtype: str = "f32", warmup: int = 0):
     """Advance an ensemble of members (MemberSpec) with the batched LBM and
     record a frame of every member every `jump` iterations.  Returns frames
-    (members, n_frames, H, W, 16) bfloat16 on the GPU (all members must share
-    one lattice size) and the ensemble's finite flags."""
+    (members, n_frames, H, W, 4) bfloat16 on the GPU (the four live channels;
+    ``expand`` makes network inputs; all members share one lattice size) and
+    the members' finite flags."""
     from .ensemble import Ensemble
     ens = Ensemble([s.build() for s in specs], dtype=dtype)
     if warmup:
         ens.step(warmup)
     H, W = ens.lattices[0].H, ens.lattices[0].W
-    frames = torch.empty((len(specs), n_frames, H, W, FRAME_CHANNELS), dtype=torch.bfloat16,
-                         device=ens.lattices[0].device)
+    frames = torch.empty((len(specs), n_frames, H, W, 4), dtype=torch.bfloat16, device=ens.lattices[0].device)
     for k in range(n_frames):
         if k:
             ens.step(jump)
         torch.cuda.current_stream().wait_stream(ens.stream)
         for m, lat in enumerate(ens.lattices):
-            frames[m, k] = member_frame(lat)
+            frames[m, k] = member_frame(lat)[..., :4]
     finite = torch.isfinite(frames.float().view(len(specs), -1)).all(dim=1)
     ens.close()
     return frames, finite
@@ -326,15 +331,15 @@ def generate_trajectories(specs, n_frames: int, jump: int = 200, dtype: str = "f
 def train(net: UNet, frames: torch.Tensor, steps: int, batch: int = 32, lr: float = 1e-3, seed: int = 0,
           log_every: int = 0):
     """AdamW on random (frame k, frame k+1) pairs of `frames`
-    (members, n_frames, H, W, 16).  Returns the loss history (host floats)."""
+    (members, n_frames, H, W, 4).  Returns the loss history (host floats)."""
     g = torch.Generator(device="cpu").manual_seed(seed)
     M, F = frames.shape[:2]
     hist = []
     for it in range(steps):
         mi = torch.randint(0, M, (batch,), generator=g)
         fi = torch.randint(0, F - 1, (batch,), generator=g)
-        x = frames[mi, fi].contiguous()
-        xn = frames[mi, fi + 1].contiguous()
+        x = expand(frames[mi, fi])
+        xn = expand(frames[mi, fi + 1])
         loss = net.loss_grad(x, xn)
         net.adamw(lr=lr)
         if log_every and (it % log_every == 0 or it == steps - 1):
@@ -351,8 +356,8 @@ def evaluate(net: UNet, frames: torch.Tensor, batch: int = 16) -> dict:
     for i in range(0, len(pairs), batch):
         mi = torch.tensor([p[0] for p in pairs[i:i + batch]])
         fi = torch.tensor([p[1] for p in pairs[i:i + batch]])
-        x = frames[mi, fi].contiguous()
-        xn = frames[mi, fi + 1].contiguous()
+        x = expand(frames[mi, fi])
+        xn = expand(frames[mi, fi + 1])
         pred = net.predict(x).float()[..., :3]
         tgt = xn.float()[..., :3]
         fl = (x[..., 3] == 0).unsqueeze(-1).float()
@@ -360,6 +365,26 @@ def evaluate(net: UNet, frames: torch.Tensor, batch: int = 16) -> dict:
         se_per += float((((x.float()[..., :3] - tgt) ** 2) * fl).sum())
         cnt += float(fl.sum()) * 3
     return {"mse_net": se_net / cnt, "mse_persistence": se_per / cnt, "gain": se_per / max(se_net, 1e-30)}
+
+
+def rollout_saturation_error(net: UNet, frames: torch.Tensor, start: int = 0, jumps: int = 5,
+                             batch: int = 16) -> list[dict]:
+    """Autoregressive surrogate rollout from frame `start` of every member of
+    `frames` (held-out LBM trajectories): per jump, the relative saturation
+    error against the LBM frame of the same iteration (mean and max over
+    members)."""
+    M = frames.shape[0]
+    errs = [[] for _ in range(jumps)]
+    for i in range(0, M, batch):
+        x = expand(frames[i:i + batch, start])
+        fluid = x[..., 3] == 0
+        for j in range(jumps):
+            x = net.predict(x)
+            sp = (((x[..., 0].float() > 0) & fluid).sum(dim=(1, 2)).float() / fluid.sum(dim=(1, 2)).float())
+            tr = frames[i:i + batch, start + j + 1, ..., 0].float()
+            st = (((tr > 0) & fluid).sum(dim=(1, 2)).float() / fluid.sum(dim=(1, 2)).float())
+            errs[j] += ((sp - st).abs() / st.clamp_min(1e-12)).tolist()
+    return [{"jump": j + 1, "mean": float(np.mean(e)), "max": float(np.max(e))} for j, e in enumerate(errs)]
 
 
 # ----------------------------------------------------------------------------
@@ -386,7 +411,7 @@ def rollout(net: UNet, lat, jumps_per_check: int = 5, checks: int = 4, jump: int
         start_it = lat.iteration
         t0 = time.perf_counter()
         saved = {k: getattr(lat, k).clone() for k in ("psi", "ux", "uy", "rho")}
-        x = frame_from_fields(lat.psi, lat.ux, lat.uy, solid).unsqueeze(0).contiguous()
+        x = frame_from_fields(lat.psi, lat.ux, lat.uy, solid).unsqueeze(0).contiguous()  # (1, H, W, 16)
         for _ in range(jumps_per_check):
             x = net.predict(x)
         psi, ux, uy = fields_from_frame(x[0])
