@@ -4,8 +4,9 @@
 // and FP32 accumulation (mma.sync m16n8k16; operand tiles staged in shared
 // memory by cp.async, fragments loaded with ldmatrix):
 //   forward / data gradient: M = pixels, N = output channels, K = 9 x input
-//     channels; a CTA computes 64 pixels x BN channels, marching over the nine
-//     taps and the input channels in chunks of BK, double-buffered;
+//     channels; a CTA computes 64 pixels x BN channels, marching over the input
+//     channels in chunks of BK and, within a chunk, over the nine taps
+//     (their input rows overlap, so the copies go through L1), double-buffered;
 //   weight gradient: M = output channels, N = input channels of one tap, K =
 //     pixels, split over pixel ranges into FP32 partials that one pass adds in
 //     a fixed order.
@@ -28,6 +29,11 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)_
 // 16-byte global -> shared copy; src_bytes = 0 writes zeros (padding)
 __device__ __forceinline__ void cp16(void* dst, const void* src, int src_bytes) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+// the same through L1: the nine taps of a chunk re-read neighbouring pixels
+__device__ __forceinline__ void cp16_l1(void* dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
                : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
@@ -122,8 +128,9 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ x
     a_x[i] = rem % W;
   }
 
+  // K order: input-channel chunk major, the nine taps of a chunk back to back
   auto load_chunk = [&](int kc, int stage) {
-    const int tap = kc / cchunks, ci0 = (kc % cchunks) * BK;
+    const int tap = kc % 9, ci0 = (kc / 9) * BK;
     const int ky = tap / 3 - 1, kx = tap % 3 - 1;
 #pragma unroll
     for (int i = 0; i < A_PER; ++i) {
@@ -132,7 +139,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ x
         const int yy = a_y[i] + ky, xx = a_x[i] + kx;
         const bool ok = a_n[i] >= 0 && yy >= 0 && yy < H && xx >= 0 && xx < W;
         const bf16* src = ok ? x + (((long long)a_n[i] * H + yy) * W + xx) * Cin + ci0 + a_sub[i] * 8 : x;
-        cp16(&As[stage][a_row[i] * C::LDS + a_sub[i] * 8], src, ok ? 16 : 0);
+        cp16_l1(&As[stage][a_row[i] * C::LDS + a_sub[i] * 8], src, ok ? 16 : 0);
       }
     }
     for (int v = tid; v < C::B_VEC; v += kThreads) {
@@ -166,10 +173,24 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ x
         const int r = wm * C::TM + mt * 16 + (lane & 15);
         ldsm_x4(af[mt], &As[st][r * C::LDS + ks * 16 + (lane >> 4) * 8]);
       }
+      if constexpr (C::NT % 2 == 0) {
+        // two n8 fragments per ldmatrix: lanes 16..31 address the second
 #pragma unroll
-      for (int nt = 0; nt < C::NT; ++nt) {
-        const int r = wn * C::TN + nt * 8 + (lane & 7);
-        ldsm_x2(bfr[nt], &Bs[st][r * C::LDS + ks * 16 + ((lane >> 3) & 1) * 8]);
+        for (int nt = 0; nt < C::NT; nt += 2) {
+          uint32_t r4[4];
+          const int r = wn * C::TN + nt * 8 + (lane & 7) + ((lane >> 4) << 3);
+          ldsm_x4(r4, &Bs[st][r * C::LDS + ks * 16 + ((lane >> 3) & 1) * 8]);
+          bfr[nt][0] = r4[0];
+          bfr[nt][1] = r4[1];
+          bfr[nt + 1][0] = r4[2];
+          bfr[nt + 1][1] = r4[3];
+        }
+      } else {
+#pragma unroll
+        for (int nt = 0; nt < C::NT; ++nt) {
+          const int r = wn * C::TN + nt * 8 + (lane & 7);
+          ldsm_x2(bfr[nt], &Bs[st][r * C::LDS + ks * 16 + ((lane >> 3) & 1) * 8]);
+        }
       }
 #pragma unroll
       for (int mt = 0; mt < C::MT; ++mt)
@@ -228,7 +249,7 @@ void conv_bk(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const f
 // ---------------------------------------------------------------------------
 template <int BM, int BN>
 struct WgCfg {
-  static constexpr int BK = 32;                              // pixels per chunk
+  static constexpr int BK = 64;                              // pixels per chunk
   static constexpr int WM = BM >= 32 ? 2 : 1;
   static constexpr int WN_MAX = 4 / WM;
   static constexpr int WN = (BN / 8) < WN_MAX ? (BN / 8) : WN_MAX;
@@ -370,7 +391,7 @@ int tile_n(int Cin) { return Cin % 64 == 0 ? 64 : (Cin % 32 == 0 ? 32 : 16); }
 
 int auto_splits(long long M, int Cin, int Cout) {
   const long long tiles = (long long)(Cout / tile_m(Cout)) * (Cin / tile_n(Cin)) * 9;
-  long long s = (2 * 152 + tiles - 1) / tiles;                 // about two waves of CTAs
+  long long s = (8 * 152 + tiles - 1) / tiles;                 // enough CTAs to fill every SM several times
   const long long max_s = (M + 1023) / 1024;                  // at least 1024 pixels per split
   if (s > max_s) s = max_s;
   if (s < 1) s = 1;
@@ -392,89 +413,155 @@ __global__ void k_flip(const bf16* __restrict__ w, int Cin, int Cout, bf16* __re
   wt[((size_t)ci * 9 + (2 - ky) * 3 + (2 - kx)) * Cout + co] = w[i];
 }
 
-__global__ void k_gelu_bwd(const bf16* __restrict__ dy, const bf16* __restrict__ z, size_t n, bf16* __restrict__ dz) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  dz[i] = __float2bfloat16_rn(__bfloat162float(dy[i]) * gelu_grad_f(__bfloat162float(z[i])));
+// 8 bfloat16 values <-> 8 floats
+struct V8 {
+  float v[8];
+};
+__device__ __forceinline__ V8 ld8(const bf16* p) {
+  const uint4 u = *reinterpret_cast<const uint4*>(p);
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+  V8 r;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float2 f = __bfloat1622float2(h[k]);
+    r.v[2 * k] = f.x;
+    r.v[2 * k + 1] = f.y;
+  }
+  return r;
+}
+__device__ __forceinline__ void st8(bf16* p, const V8& r) {
+  uint4 u;
+  __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&u);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) h[k] = __floats2bfloat162_rn(r.v[2 * k], r.v[2 * k + 1]);
+  *reinterpret_cast<uint4*>(p) = u;
 }
 
-constexpr int kBiasBlocks = 256;
+__global__ void k_gelu_bwd(const bf16* __restrict__ dy, const bf16* __restrict__ z, size_t n8, bf16* __restrict__ dz) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n8) return;
+  V8 a = ld8(dy + 8 * i);
+  const V8 b = ld8(z + 8 * i);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a.v[k] *= gelu_grad_f(b.v[k]);
+  st8(dz + 8 * i, a);
+}
 
-__global__ void k_bias_partial(const bf16* __restrict__ dz, size_t P, int C, float* __restrict__ partial) {
-  const size_t per = (P + gridDim.x - 1) / gridDim.x;
-  const size_t lo = (size_t)blockIdx.x * per, hi = min(P, lo + per);
+constexpr int kBiasBlocks = 512;
+constexpr int kBiasThreads = 256;
+
+// Per-block channel sums of dz over a pixel range: each thread owns 8
+// channels of every (kBiasThreads / (C/8))-th pixel, then the block adds its
+// rows in a fixed order.  C % 8 == 0, C <= 8 * kBiasThreads.
+__global__ void __launch_bounds__(kBiasThreads) k_bias_partial(const bf16* __restrict__ dz, size_t P, int C,
+                                                               float* __restrict__ partial) {
+  __shared__ float s[kBiasThreads * 8];
+  const int vpp = C / 8, ppi = kBiasThreads / vpp;
+  const int lv = threadIdx.x % vpp, lp = threadIdx.x / vpp;
+  float acc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  if (lp < ppi) {
+    const size_t per = (P + gridDim.x - 1) / gridDim.x;
+    const size_t lo = (size_t)blockIdx.x * per, hi = min(P, lo + per);
+    for (size_t p = lo + lp; p < hi; p += ppi) {
+      const V8 v = ld8(dz + p * C + 8 * lv);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) acc[k] += v.v[k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s[threadIdx.x * 8 + k] = acc[k];
+  __syncthreads();
   for (int c = threadIdx.x; c < C; c += blockDim.x) {
-    float s = 0.0f;
-    for (size_t p = lo; p < hi; ++p) s += __bfloat162float(dz[p * C + c]);
-    partial[(size_t)blockIdx.x * C + c] = s;
+    const int v = c / 8, k = c % 8;
+    float t = 0.0f;
+    for (int q = 0; q < ppi; ++q) t += s[(q * vpp + v) * 8 + k];
+    partial[(size_t)blockIdx.x * C + c] = t;
   }
 }
 
+// 8 channels per thread: i indexes (output pixel, channel group)
 __global__ void k_pool2(const bf16* __restrict__ x, int N, int H, int W, int C, bf16* __restrict__ y) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int h = H / 2, w = W / 2;
-  const size_t n_out = (size_t)N * h * w * C;
+  const int h = H / 2, w = W / 2, cg = C / 8;
+  const size_t n_out = (size_t)N * h * w * cg;
   if (i >= n_out) return;
-  const int c = (int)(i % C);
-  const size_t pix = i / C;
+  const int c = (int)(i % cg) * 8;
+  const size_t pix = i / cg;
   const int xo = (int)(pix % w), yo = (int)((pix / w) % h), n = (int)(pix / ((size_t)w * h));
   const size_t b = (((size_t)n * H + 2 * yo) * W + 2 * xo) * C + c;
-  const float s = (__bfloat162float(x[b]) + __bfloat162float(x[b + C])) +
-                  (__bfloat162float(x[b + (size_t)W * C]) + __bfloat162float(x[b + (size_t)W * C + C]));
-  y[i] = __float2bfloat16_rn(0.25f * s);
+  const V8 a = ld8(x + b), bb = ld8(x + b + C), cc = ld8(x + b + (size_t)W * C), d = ld8(x + b + (size_t)W * C + C);
+  V8 r;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) r.v[k] = 0.25f * ((a.v[k] + bb.v[k]) + (cc.v[k] + d.v[k]));
+  st8(y + pix * C + c, r);
 }
 
 __global__ void k_pool2_bwd(const bf16* __restrict__ dy, int N, int H, int W, int C, bf16* __restrict__ dx) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t n_in = (size_t)N * H * W * C;
+  const int cg = C / 8;
+  const size_t n_in = (size_t)N * H * W * cg;
   if (i >= n_in) return;
-  const int c = (int)(i % C);
-  const size_t pix = i / C;
+  const int c = (int)(i % cg) * 8;
+  const size_t pix = i / cg;
   const int xx = (int)(pix % W), yy = (int)((pix / W) % H), n = (int)(pix / ((size_t)W * H));
-  const size_t j = (((size_t)n * (H / 2) + yy / 2) * (W / 2) + xx / 2) * C + c;
-  dx[i] = __float2bfloat16_rn(0.25f * __bfloat162float(dy[j]));
+  V8 r = ld8(dy + (((size_t)n * (H / 2) + yy / 2) * (W / 2) + xx / 2) * C + c);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) r.v[k] *= 0.25f;
+  st8(dx + pix * C + c, r);
 }
 
 __global__ void k_up2(const bf16* __restrict__ x, int N, int h, int w, int C, bf16* __restrict__ y, int Cy, int coff) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t n_out = (size_t)N * 2 * h * 2 * w * C;
+  const int cg = C / 8;
+  const size_t n_out = (size_t)N * 2 * h * 2 * w * cg;
   if (i >= n_out) return;
-  const int c = (int)(i % C);
-  const size_t pix = i / C;
+  const int c = (int)(i % cg) * 8;
+  const size_t pix = i / cg;
   const int W = 2 * w, H = 2 * h;
   const int xx = (int)(pix % W), yy = (int)((pix / W) % H), n = (int)(pix / ((size_t)W * H));
-  y[pix * Cy + coff + c] = x[(((size_t)n * h + yy / 2) * w + xx / 2) * C + c];
+  *reinterpret_cast<uint4*>(y + pix * Cy + coff + c) =
+      *reinterpret_cast<const uint4*>(x + (((size_t)n * h + yy / 2) * w + xx / 2) * C + c);
 }
 
 __global__ void k_up2_bwd(const bf16* __restrict__ dy, int N, int h, int w, int Cy, int coff, int C,
                           bf16* __restrict__ dx) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t n_in = (size_t)N * h * w * C;
+  const int cg = C / 8;
+  const size_t n_in = (size_t)N * h * w * cg;
   if (i >= n_in) return;
-  const int c = (int)(i % C);
-  const size_t pix = i / C;
+  const int c = (int)(i % cg) * 8;
+  const size_t pix = i / cg;
   const int xo = (int)(pix % w), yo = (int)((pix / w) % h), n = (int)(pix / ((size_t)w * h));
   const int W = 2 * w;
   const size_t b = (((size_t)n * 2 * h + 2 * yo) * W + 2 * xo) * Cy + coff + c;
-  const float s = (__bfloat162float(dy[b]) + __bfloat162float(dy[b + Cy])) +
-                  (__bfloat162float(dy[b + (size_t)W * Cy]) + __bfloat162float(dy[b + (size_t)W * Cy + Cy]));
-  dx[i] = __float2bfloat16_rn(s);
+  const V8 a = ld8(dy + b), bb = ld8(dy + b + Cy), cc = ld8(dy + b + (size_t)W * Cy),
+           d = ld8(dy + b + (size_t)W * Cy + Cy);
+  V8 r;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) r.v[k] = (a.v[k] + bb.v[k]) + (cc.v[k] + d.v[k]);
+  st8(dx + pix * C + c, r);
 }
 
 __global__ void k_copy_ch(const bf16* __restrict__ src, size_t P, int Cs, bf16* __restrict__ dst, int Cd, int coff) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P * Cs) return;
-  const size_t p = i / Cs;
-  const int c = (int)(i % Cs);
-  dst[p * Cd + coff + c] = src[i];
+  const int cg = Cs / 8;
+  if (i >= P * cg) return;
+  const size_t p = i / cg;
+  const int c = (int)(i % cg) * 8;
+  *reinterpret_cast<uint4*>(dst + p * Cd + coff + c) = *reinterpret_cast<const uint4*>(src + p * Cs + c);
 }
 
 __global__ void k_add_ch(const bf16* __restrict__ src, size_t P, int Cs, int coff, int C, bf16* __restrict__ dst) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P * C) return;
-  const size_t p = i / C;
-  const int c = (int)(i % C);
-  dst[i] = __float2bfloat16_rn(__bfloat162float(dst[i]) + __bfloat162float(src[p * Cs + coff + c]));
+  const int cg = C / 8;
+  if (i >= P * cg) return;
+  const size_t p = i / cg;
+  const int c = (int)(i % cg) * 8;
+  V8 a = ld8(dst + p * C + c);
+  const V8 b = ld8(src + p * Cs + coff + c);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a.v[k] += b.v[k];
+  st8(dst + p * C + c, a);
 }
 
 constexpr int kLossBlocks = 512;
@@ -551,7 +638,8 @@ int sg_conv3x3(const void* x, int N, int H, int W, int Cin, const void* w, const
   FD_REQUIRE(((uintptr_t)x | (uintptr_t)w) % 16 == 0, FD_ERR_ARG, "sg_conv3x3: x and w must be 16-byte aligned");
   cudaStream_t s = as_stream(stream);
   const bf16 *xb = (const bf16*)x, *wb = (const bf16*)w;
-  if (Cin % 32 == 0) conv_bk<32>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
+  if (Cin % 64 == 0) conv_bk<64>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
+  else if (Cin % 32 == 0) conv_bk<32>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
   else conv_bk<16>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
   return check_launch("sg_conv3x3");
 }
@@ -578,7 +666,7 @@ int sg_conv3x3_wgrad(const void* x, const void* dz, int N, int H, int W, int Cin
   const size_t n = (size_t)Cout * 9 * Cin;
   FD_REQUIRE((size_t)splits * n <= partial_floats, FD_ERR_ARG, "sg_conv3x3_wgrad: partial buffer too small");
   long long chunk = (M + splits - 1) / splits;
-  chunk = (chunk + 31) / 32 * 32;
+  chunk = (chunk + 63) / 64 * 64;
   cudaStream_t s = as_stream(stream);
   const bf16 *xb = (const bf16*)x, *db = (const bf16*)dz;
   switch (tile_m(Cout)) {
@@ -593,56 +681,61 @@ int sg_conv3x3_wgrad(const void* x, const void* dz, int N, int H, int W, int Cin
 size_t sg_bias_partial_floats(int C) { return (size_t)kBiasBlocks * (C > 0 ? C : 0); }
 
 int sg_bias_grad(const void* dz, size_t P, int C, float* db, float* partial, void* stream) {
-  FD_REQUIRE(dz && db && partial && C > 0, FD_ERR_ARG, "sg_bias_grad: bad arguments");
+  FD_REQUIRE(dz && db && partial && C > 0 && C % 8 == 0 && C <= 8 * kBiasThreads, FD_ERR_ARG,
+             "sg_bias_grad: bad arguments");
   cudaStream_t s = as_stream(stream);
-  k_bias_partial<<<kBiasBlocks, 128, 0, s>>>((const bf16*)dz, P, C, partial);
+  k_bias_partial<<<kBiasBlocks, kBiasThreads, 0, s>>>((const bf16*)dz, P, C, partial);
   k_sum_partials<<<ew_blocks((size_t)C), kEw, 0, s>>>(partial, kBiasBlocks, (size_t)C, db);
   return check_launch("sg_bias_grad");
 }
 
 int sg_gelu_bwd(const void* dy, const void* z, size_t n, void* dz, void* stream) {
-  FD_REQUIRE(dy && z && dz, FD_ERR_ARG, "sg_gelu_bwd: NULL pointer");
-  k_gelu_bwd<<<ew_blocks(n), kEw, 0, as_stream(stream)>>>((const bf16*)dy, (const bf16*)z, n, (bf16*)dz);
+  FD_REQUIRE(dy && z && dz && n % 8 == 0, FD_ERR_ARG, "sg_gelu_bwd: bad arguments (n must be a multiple of 8)");
+  k_gelu_bwd<<<ew_blocks(n / 8), kEw, 0, as_stream(stream)>>>((const bf16*)dy, (const bf16*)z, n / 8, (bf16*)dz);
   return check_launch("sg_gelu_bwd");
 }
 
 int sg_pool2(const void* x, int N, int H, int W, int C, void* y, void* stream) {
-  FD_REQUIRE(x && y && H % 2 == 0 && W % 2 == 0, FD_ERR_ARG, "sg_pool2: bad arguments");
-  const size_t n = (size_t)N * (H / 2) * (W / 2) * C;
+  FD_REQUIRE(x && y && H % 2 == 0 && W % 2 == 0 && C % 8 == 0, FD_ERR_ARG, "sg_pool2: bad arguments");
+  const size_t n = (size_t)N * (H / 2) * (W / 2) * (C / 8);
   k_pool2<<<ew_blocks(n), kEw, 0, as_stream(stream)>>>((const bf16*)x, N, H, W, C, (bf16*)y);
   return check_launch("sg_pool2");
 }
 
 int sg_pool2_bwd(const void* dy, int N, int H, int W, int C, void* dx, void* stream) {
-  FD_REQUIRE(dy && dx && H % 2 == 0 && W % 2 == 0, FD_ERR_ARG, "sg_pool2_bwd: bad arguments");
-  const size_t n = (size_t)N * H * W * C;
+  FD_REQUIRE(dy && dx && H % 2 == 0 && W % 2 == 0 && C % 8 == 0, FD_ERR_ARG, "sg_pool2_bwd: bad arguments");
+  const size_t n = (size_t)N * H * W * (C / 8);
   k_pool2_bwd<<<ew_blocks(n), kEw, 0, as_stream(stream)>>>((const bf16*)dy, N, H, W, C, (bf16*)dx);
   return check_launch("sg_pool2_bwd");
 }
 
 int sg_up2(const void* x, int N, int h, int w, int C, void* y, int Cy, int coff, void* stream) {
-  FD_REQUIRE(x && y && coff >= 0 && coff + C <= Cy, FD_ERR_ARG, "sg_up2: bad arguments");
-  const size_t n = (size_t)N * 4 * h * w * C;
+  FD_REQUIRE(x && y && coff >= 0 && coff + C <= Cy && C % 8 == 0 && Cy % 8 == 0 && coff % 8 == 0, FD_ERR_ARG,
+             "sg_up2: bad arguments");
+  const size_t n = (size_t)N * 4 * h * w * (C / 8);
   k_up2<<<ew_blocks(n), kEw, 0, as_stream(stream)>>>((const bf16*)x, N, h, w, C, (bf16*)y, Cy, coff);
   return check_launch("sg_up2");
 }
 
 int sg_up2_bwd(const void* dy, int N, int h, int w, int Cy, int coff, int C, void* dx, void* stream) {
-  FD_REQUIRE(dy && dx && coff >= 0 && coff + C <= Cy, FD_ERR_ARG, "sg_up2_bwd: bad arguments");
-  const size_t n = (size_t)N * h * w * C;
+  FD_REQUIRE(dy && dx && coff >= 0 && coff + C <= Cy && C % 8 == 0 && Cy % 8 == 0 && coff % 8 == 0, FD_ERR_ARG,
+             "sg_up2_bwd: bad arguments");
+  const size_t n = (size_t)N * h * w * (C / 8);
   k_up2_bwd<<<ew_blocks(n), kEw, 0, as_stream(stream)>>>((const bf16*)dy, N, h, w, Cy, coff, C, (bf16*)dx);
   return check_launch("sg_up2_bwd");
 }
 
 int sg_copy_channels(const void* src, size_t P, int Cs, void* dst, int Cd, int coff, void* stream) {
-  FD_REQUIRE(src && dst && coff >= 0 && coff + Cs <= Cd, FD_ERR_ARG, "sg_copy_channels: bad arguments");
-  k_copy_ch<<<ew_blocks(P * Cs), kEw, 0, as_stream(stream)>>>((const bf16*)src, P, Cs, (bf16*)dst, Cd, coff);
+  FD_REQUIRE(src && dst && coff >= 0 && coff + Cs <= Cd && Cs % 8 == 0 && Cd % 8 == 0 && coff % 8 == 0, FD_ERR_ARG,
+             "sg_copy_channels: bad arguments");
+  k_copy_ch<<<ew_blocks(P * (Cs / 8)), kEw, 0, as_stream(stream)>>>((const bf16*)src, P, Cs, (bf16*)dst, Cd, coff);
   return check_launch("sg_copy_channels");
 }
 
 int sg_add_channels(const void* src, size_t P, int Cs, int coff, int C, void* dst, void* stream) {
-  FD_REQUIRE(src && dst && coff >= 0 && coff + C <= Cs, FD_ERR_ARG, "sg_add_channels: bad arguments");
-  k_add_ch<<<ew_blocks(P * C), kEw, 0, as_stream(stream)>>>((const bf16*)src, P, Cs, coff, C, (bf16*)dst);
+  FD_REQUIRE(src && dst && coff >= 0 && coff + C <= Cs && C % 8 == 0 && Cs % 8 == 0 && coff % 8 == 0, FD_ERR_ARG,
+             "sg_add_channels: bad arguments");
+  k_add_ch<<<ew_blocks(P * (C / 8)), kEw, 0, as_stream(stream)>>>((const bf16*)src, P, Cs, coff, C, (bf16*)dst);
   return check_launch("sg_add_channels");
 }
 

@@ -374,6 +374,7 @@ def rollout_saturation_error(net: UNet, frames: torch.Tensor, start: int = 0, ju
     error against the LBM frame of the same iteration (mean and max over
     members)."""
     M = frames.shape[0]
+    jumps = min(jumps, frames.shape[1] - 1 - start)
     errs = [[] for _ in range(jumps)]
     for i in range(0, M, batch):
         x = expand(frames[i:i + batch, start])
