@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(PKG, "_lib", "libfdlbm.so")
 
 FD_OK = 0
 FD_F64, FD_F32, FD_F16, FD_BF16 = 0, 1, 2, 3
-FD_VARIANT_PERIODIC, FD_VARIANT_WALLS = 0, 1
+FD_VARIANT_PERIODIC, FD_VARIANT_WALLS, FD_VARIANT_PERIODIC_XY = 0, 1, 2
 FD_INIT_MU, FD_INIT_UY, FD_INIT_VELOCITY = 1, 2, 4
 FD_ROUND_NEAREST, FD_ROUND_STOCHASTIC = 0, 1
 ROUNDING = {"nearest": FD_ROUND_NEAREST, "stochastic": FD_ROUND_STOCHASTIC}
@@ -35,7 +35,7 @@ class fd_params(C.Structure):
     _fields_ = [("H", C.c_int32), ("W", C.c_int32), ("variant", C.c_int32), ("flags", C.c_uint32),
                 ("tau", C.c_double), ("eta_n", C.c_double), ("M", C.c_double), ("a", C.c_double),
                 ("kappa", C.c_double), ("gamma", C.c_double), ("psi_wall", C.c_double),
-                ("outlet_coef", C.c_double)]
+                ("outlet_coef", C.c_double), ("force_x", C.c_double), ("force_y", C.c_double)]
 
 
 class fd_storage(C.Structure):

@@ -171,6 +171,8 @@ int fd_batch_create(const fd_instance* inst, int n, const fd_storage* st, int ro
   FD_REQUIRE(rows_per_strip >= 1, FD_ERR_ARG, "fd_batch_create: rows per strip must be positive");
   for (int i = 0; i < n; ++i) {
     if (int r = check_params(&inst[i].prm)) return r;
+    FD_REQUIRE(inst[i].prm.variant != FD_VARIANT_PERIODIC_XY, FD_ERR_SHAPE,
+               "fd_batch_create: instance %d uses the periodic-xy variant (reference-order kernels only)", i);
     FD_REQUIRE(inst[i].prm.W % 8 == 0, FD_ERR_SHAPE, "fd_batch_create: instance %d width %d is not a multiple of 8",
                i, inst[i].prm.W);
     FD_REQUIRE(inst[i].mask && inst[i].inlet_ux && inst[i].pop_a && inst[i].pop_b && inst[i].side_a &&

@@ -51,6 +51,8 @@ struct Coef {
   T wsum_out;    // w3 + w6 + w7
   T wsum_68;     // w6 + w8                        (fingering.py:346)
   T wsum_57;     // w5 + w7                        (fingering.py:362)
+  T bx, by;      // body force per unit mass (FD_VARIANT_PERIODIC_XY; no reference counterpart)
+  int body;      // 1: add the body force to the velocity and the forcing term
 };
 
 template <typename T>
@@ -76,6 +78,9 @@ inline Coef<T> make_coef(const fd_params& p) {
   c.wsum_out = (T)((w[3] + w[6]) + w[7]);
   c.wsum_68 = (T)(w[6] + w[8]);
   c.wsum_57 = (T)(w[5] + w[7]);
+  c.body = p.variant == FD_VARIANT_PERIODIC_XY;
+  c.bx = (T)(c.body ? p.force_x : 0.0);
+  c.by = (T)(c.body ? p.force_y : 0.0);
   return c;
 }
 

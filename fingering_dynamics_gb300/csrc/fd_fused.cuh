@@ -99,17 +99,19 @@ __device__ __forceinline__ T rho_inlet_row(const FusedArgs<T>& a, size_t P, int 
   return inlet_rho(fn, (T)a.inlet_ux[yn], a.side_in[0 * a.H + yn], a.side_in[2 * a.H + yn]);
 }
 
-// psi of a pulled row (x ghosts +1 / -1, psi_wall on solid cells)
+// psi of a pulled row (x ghosts +1 / -1, psi_wall on solid cells; the
+// halo lanes' wrapped cells for FD_VARIANT_PERIODIC_XY)
 template <typename T, int VEC>
 __device__ __forceinline__ void psi_row(const FusedArgs<T>& a, int x0, const uint16_t (&mb)[VEC],
                                         const T (&g)[9][VEC], T (&psi)[VEC]) {
+  const bool ghosts = a.variant != FD_VARIANT_PERIODIC_XY;
 #pragma unroll
   for (int k = 0; k < VEC; ++k) {
     const int x = x0 + k;
     T s = g[0][k];
 #pragma unroll
     for (int i = 1; i < 9; ++i) s = s + g[i][k];
-    psi[k] = (x < 0) ? T(1) : (x >= a.W) ? T(-1) : ((mb[k] & SOLID) ? a.c.psi_wall : s);
+    psi[k] = (ghosts && x < 0) ? T(1) : (ghosts && x >= a.W) ? T(-1) : ((mb[k] & SOLID) ? a.c.psi_wall : s);
   }
 }
 

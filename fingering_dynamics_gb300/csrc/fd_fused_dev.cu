@@ -93,6 +93,9 @@ int fd_fused_step_packed(const fd_params* prm, const fd_storage* st, const uint1
                          void* pop_a, void* pop_b, void* side_a, void* side_b, int nsteps, int rows_per_warp,
                          void* stream) {
   if (int r = check_params(prm)) return r;
+  FD_REQUIRE(prm->variant != FD_VARIANT_PERIODIC_XY, FD_ERR_SHAPE,
+             "fd_fused_step_packed: the periodic-xy body-force variant runs on the reference-order kernels "
+             "(fd_fused_step, FP64 / FP32) only");
   if (int r = check_storage(st)) return r;
   FD_REQUIRE(mask && inlet_ux && pop_a && pop_b && side_a && side_b, FD_ERR_ARG, "fd_fused_step_packed: NULL pointer");
   FD_REQUIRE(pop_a != pop_b && side_a != side_b, FD_ERR_ARG, "fd_fused_step_packed: ping-pong buffers must differ");

@@ -33,8 +33,9 @@ inline int check_launch(const char* what) {
 inline int check_params(const fd_params* p) {
   FD_REQUIRE(p != nullptr, FD_ERR_ARG, "params is NULL");
   FD_REQUIRE(p->H >= 2 && p->W >= 2, FD_ERR_SHAPE, "lattice %dx%d too small", p->H, p->W);
-  FD_REQUIRE(p->variant == FD_VARIANT_PERIODIC || p->variant == FD_VARIANT_WALLS, FD_ERR_ARG,
-             "unknown variant %d", p->variant);
+  FD_REQUIRE(p->variant == FD_VARIANT_PERIODIC || p->variant == FD_VARIANT_WALLS ||
+                 p->variant == FD_VARIANT_PERIODIC_XY,
+             FD_ERR_ARG, "unknown variant %d", p->variant);
   FD_REQUIRE(p->variant != FD_VARIANT_WALLS || p->H >= 3, FD_ERR_SHAPE,
              "the walled variant needs H >= 3 (walls act on rows 1 and H-2)");
   return FD_OK;

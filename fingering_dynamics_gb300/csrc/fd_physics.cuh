@@ -74,6 +74,14 @@ __device__ __forceinline__ T velocity_of(T mom, T mu, T grad, T rho) {
   return (mom + ((mu * grad) / T(2))) / rho;
 }
 
+// the same with half the body force density rho b added (Guo forcing; the
+// FD_VARIANT_PERIODIC_XY extension), or velocity_of when c.body == 0
+template <typename T>
+__device__ __forceinline__ T velocity_c(const Coef<T>& c, T mom, T mu, T grad, T rho, T b) {
+  if (!c.body) return velocity_of(mom, mu, grad, rho);
+  return ((mom + ((mu * grad) / T(2))) + ((rho * b) / T(2))) / rho;
+}
+
 // Macroscopic fields of one fluid cell from its populations, psi and the
 // psi stencils, in the order of fingering_periodic.py:470-479.
 template <typename T>
@@ -84,8 +92,8 @@ __device__ __forceinline__ Macro<T> macros_of(const Coef<T>& c, const T (&f)[9],
   m.gx = gx;
   m.gy = gy;
   m.mu = chem_pot(c, psi, lap);
-  m.ux = velocity_of(mom_x(f), m.mu, gx, m.rho);
-  m.uy = velocity_of(mom_y(f), m.mu, gy, m.rho);
+  m.ux = velocity_c(c, mom_x(f), m.mu, gx, m.rho, c.bx);
+  m.uy = velocity_c(c, mom_y(f), m.mu, gy, m.rho, c.by);
   m.p = pressure_of(c, m.rho, psi, m.mu);
   m.tau_mix = mix_tau_of(c, m.rho, psi);
   return m;
@@ -118,8 +126,10 @@ __device__ __forceinline__ void dir_terms(const Coef<T>& c, const Macro<T>& m, c
   const T q = (T(3) * eu + T(4.5) * (eu * eu)) - T(1.5) * t.usq;
   feq = c.w[I] * ((I == 0 ? t.A0 : t.A18) + m.rho * q);
   geq = c.w[I] * ((I == 0 ? t.B0 : t.B18) + m.psi * q);
-  F = ((m.mu * c.w[I]) * t.pref) *
-      ((((ex - m.ux) * T(3)) + ((ex * eu) * T(9))) * m.gx + (((ey - m.uy) * T(3)) + ((ey * eu) * T(9))) * m.gy);
+  const T Ax = ((ex - m.ux) * T(3)) + ((ex * eu) * T(9));
+  const T Ay = ((ey - m.uy) * T(3)) + ((ey * eu) * T(9));
+  F = ((m.mu * c.w[I]) * t.pref) * (Ax * m.gx + Ay * m.gy);
+  if (c.body) F = F + ((m.rho * c.w[I]) * t.pref) * (Ax * c.bx + Ay * c.by);  // body force density rho b
 }
 
 template <int I, typename T>

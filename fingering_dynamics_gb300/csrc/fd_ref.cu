@@ -38,6 +38,7 @@ inline dim3 grid_cells(const Shape& s) { return dim3((unsigned)((s.P + kBlock - 
 // (fingering_periodic.py:216-217), +1 / -1 ghost columns left / right
 // (fingering_periodic.py:94-95), y wrapped (fingering_periodic.py, np.roll)
 // or psi_wall ghost rows including their corners (fingering.py:102,224).
+// FD_VARIANT_PERIODIC_XY wraps x as well.
 template <typename T>
 __device__ __forceinline__ T psi_nb(const T* __restrict__ psi, const uint16_t* __restrict__ mask, const Shape& s,
                                     T psi_wall, int x, int y) {
@@ -45,8 +46,12 @@ __device__ __forceinline__ T psi_nb(const T* __restrict__ psi, const uint16_t* _
     if (s.variant == FD_VARIANT_WALLS) return psi_wall;
     y = wrap(y, s.H);
   }
-  if (x < 0) return T(1);
-  if (x >= s.W) return T(-1);
+  if (s.variant == FD_VARIANT_PERIODIC_XY) {
+    x = wrap(x, s.W);
+  } else {
+    if (x < 0) return T(1);
+    if (x >= s.W) return T(-1);
+  }
   const size_t q = (size_t)y * s.W + x;
   return (mask[q] & SOLID) ? psi_wall : psi[q];
 }
@@ -303,8 +308,8 @@ __global__ void k_macros(Shape s, Coef<T> c, const uint16_t* __restrict__ mask, 
   const T rho = F.rho[q], psi = F.psi[q];
   const T mu = chem_pot(c, psi, lap);
   F.mu[q] = mu;
-  F.ux[q] = velocity_of(mom_x(v), mu, gx, rho);
-  F.uy[q] = velocity_of(mom_y(v), mu, gy, rho);
+  F.ux[q] = velocity_c(c, mom_x(v), mu, gx, rho, c.bx);
+  F.uy[q] = velocity_c(c, mom_y(v), mu, gy, rho, c.by);
   F.p[q] = pressure_of(c, rho, psi, mu);
   F.mix_tau[q] = mix_tau_of(c, rho, psi);
 }
@@ -336,8 +341,14 @@ __global__ void k_field(Shape s, Coef<T> c, int which, const uint16_t* __restric
   switch (which) {
     case FD_FIELD_RHO: load_cell(F.f, s.P, q, v); out[q] = sum9(v); return;
     case FD_FIELD_MU: out[q] = chem_pot(c, F.psi[q], F.np2[q]); return;
-    case FD_FIELD_UX: load_cell(F.f, s.P, q, v); out[q] = velocity_of(mom_x(v), F.mu[q], F.npx[q], F.rho[q]); return;
-    case FD_FIELD_UY: load_cell(F.f, s.P, q, v); out[q] = velocity_of(mom_y(v), F.mu[q], F.npy[q], F.rho[q]); return;
+    case FD_FIELD_UX:
+      load_cell(F.f, s.P, q, v);
+      out[q] = velocity_c(c, mom_x(v), F.mu[q], F.npx[q], F.rho[q], c.bx);
+      return;
+    case FD_FIELD_UY:
+      load_cell(F.f, s.P, q, v);
+      out[q] = velocity_c(c, mom_y(v), F.mu[q], F.npy[q], F.rho[q], c.by);
+      return;
     case FD_FIELD_P: out[q] = pressure_of(c, F.rho[q], F.psi[q], F.mu[q]); return;
     case FD_FIELD_MIX_TAU: out[q] = mix_tau_of(c, F.rho[q], F.psi[q]); return;
     default: return;

@@ -12,6 +12,7 @@ namespace fd {
 // g part of zou_he_boundary_inlet/outlet at one cell.
 template <typename T>
 __device__ __forceinline__ void zou_he_g(const Coef<T>& c, int variant, int H, int W, int x, int y, T (&g)[9]) {
+  if (variant == FD_VARIANT_PERIODIC_XY) return;  // no inlet / outlet
   if (x == 0) {
     if (variant == FD_VARIANT_WALLS) {
       if (y == 0) inlet_corner_bottom_g(c, g);
@@ -36,6 +37,7 @@ __device__ __forceinline__ void zou_he_g(const Coef<T>& c, int variant, int H, i
 template <typename T>
 __device__ __forceinline__ void zou_he_f(const Coef<T>& c, int variant, int H, int W, int x, int y, T (&f)[9],
                                          T ux, T gx, T gy, T mu, T rho_nb) {
+  if (variant == FD_VARIANT_PERIODIC_XY) return;  // no inlet / outlet
   if (x == 0) {
     if (variant == FD_VARIANT_WALLS && y == 0) inlet_corner_bottom_f(f, rho_nb);
     else if (variant == FD_VARIANT_WALLS && y == H - 1) inlet_corner_top_f(f, rho_nb);

@@ -391,6 +391,29 @@ def build_geometry(H: int, W: int, rects=(), circles=(), walls: bool = False) ->
                     list(rects), list(circles))
 
 
+def square_blocks(H: int, W: int, n: int, side: int, seed: int, gap: int = 2, margin: int = 2,
+                  max_tries: int = 100000):
+    """``n`` non-overlapping squares of ``side`` cells placed uniformly at
+    random from a seeded generator, at least ``gap`` free cells apart and
+    ``margin`` cells from the lattice edges; ``setblock`` corner pairs
+    (inclusive, create_block.py:395-407)."""
+    rng = np.random.default_rng(seed)
+    occ = np.zeros((H, W), dtype=bool)
+    rects = []
+    tries = 0
+    while len(rects) < n and tries < max_tries:
+        tries += 1
+        x0 = int(rng.integers(margin, W - margin - side + 1))
+        y0 = int(rng.integers(margin, H - margin - side + 1))
+        if occ[max(y0 - gap, 0):y0 + side + gap, max(x0 - gap, 0):x0 + side + gap].any():
+            continue
+        occ[y0:y0 + side, x0:x0 + side] = True
+        rects.append(((x0, y0), (x0 + side - 1, y0 + side - 1)))
+    if len(rects) < n:
+        raise ValueError(f"placed only {len(rects)} of {n} squares")
+    return rects
+
+
 def random_blocks(H: int, W: int, porosity: float, rmin: int, rmax: int, seed: int,
                   kinds=("circle", "square"), gap: int = 2, x_margin: int = 0,
                   max_tries: int = 200000, max_blocks: int | None = None):

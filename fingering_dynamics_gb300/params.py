@@ -23,8 +23,9 @@ import numpy as np
 
 VARIANT_PERIODIC = 0   # fingering_periodic.py: periodic in y, Gaussian inlet, outlet coefficient 2/3
 VARIANT_WALLS = 1      # fingering.py: psi_wall ghost rows, wall rows 1 and H-2, plug inlet, corners, 1.5
+VARIANT_PERIODIC_XY = 2  # extension: periodic in x and y, body force, no inlet / outlet
 
-_VARIANTS = {"periodic": VARIANT_PERIODIC, "walls": VARIANT_WALLS}
+_VARIANTS = {"periodic": VARIANT_PERIODIC, "walls": VARIANT_WALLS, "periodic_xy": VARIANT_PERIODIC_XY}
 
 
 @dataclass
@@ -57,6 +58,8 @@ class LBMParams:
     init_mu: bool = False             # fingering.py:122 computes mu before the equilibria
     init_uy: bool = False             # fingering.py:123 computes u_y (with f = 0) before the equilibria
     inlet_ux: np.ndarray | None = field(default=None, repr=False)
+    force_x: float = 0.0              # body force per unit mass, variant "periodic_xy" only
+    force_y: float = 0.0
 
     def __post_init__(self):
         if self.variant not in _VARIANTS:
@@ -141,6 +144,27 @@ def walls_reference_params(H: int = 380, W: int = 380, psi_wall: float = -1.0, P
     return LBMParams(H=H, W=W, variant="walls", tau=tau, eta_n=Eta_n, M=M, a=a, kappa=kappa,
                      gamma=gamma, psi_wall=psi_wall, u0=u0, outlet_coef=1.5, inlet="plug",
                      slab=5, init_mu=True, init_uy=True)
+
+
+def periodic_xy_params(H: int = 128, W: int = 256, tau_inv: float = 0.6, tau_def: float = 1.0, sigma: float = 1e-3,
+                       contact_angle_deg: float = 60.0, force_x: float = 1e-5, gamma: float = 1.0, slab: int = 32,
+                       xi: float = 2.0, tau_g: float | None = None) -> LBMParams:
+    """The fully periodic, body-force-driven configuration (an extension with
+    no reference counterpart: the reference always has a Zou-He inlet and
+    outlet and no body force).  Viscosities from the relaxation times as in
+    :func:`from_relaxation_times`; kappa, a from sigma (fingering_periodic.py:
+    37-39); psi_wall from the contact-angle calibration; the mobility gamma is
+    given directly (the reference's rule needs an inlet speed); invading fluid
+    on x < slab."""
+    from .calibration import psi_wall_for_angle
+    tau = (1 / (3.0 - math.sqrt(3))) if tau_g is None else tau_g
+    eta_n = (tau_inv - 0.5) / 3.0
+    M = (tau_def - 0.5) / (tau_inv - 0.5)
+    kappa = 0.75 * sigma * xi
+    a = -2.0 * kappa / (xi ** 2)
+    return LBMParams(H=H, W=W, variant="periodic_xy", tau=tau, eta_n=eta_n, M=M, a=a, kappa=kappa, gamma=gamma,
+                     psi_wall=psi_wall_for_angle(contact_angle_deg), u0=0.0, outlet_coef=2 / 3, inlet="plug",
+                     slab=slab, force_x=force_x, force_y=0.0)
 
 
 def from_relaxation_times(H: int, W: int, tau_inv: float, tau_def: float, sigma: float,

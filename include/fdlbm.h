@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define FDLBM_ABI_VERSION 2
+#define FDLBM_ABI_VERSION 3
 
 enum fd_status {
   FD_OK = 0,
@@ -46,7 +46,10 @@ enum fd_dtype { FD_F64 = 0, FD_F32 = 1, FD_F16 = 2, FD_BF16 = 3 };
 
 enum fd_variant {
   FD_VARIANT_PERIODIC = 0, /* fingering_periodic.py: y periodic, Gaussian inlet, outlet 2/3 */
-  FD_VARIANT_WALLS = 1     /* fingering.py: psi_wall ghost rows, walls on rows 1 and H-2, corners, outlet 1.5 */
+  FD_VARIANT_WALLS = 1,    /* fingering.py: psi_wall ghost rows, walls on rows 1 and H-2, corners, outlet 1.5 */
+  FD_VARIANT_PERIODIC_XY = 2 /* extension, no reference counterpart: periodic in x and y (no Zou-He, no x ghost
+                                columns) with the body force (force_x, force_y) per unit mass on both fluids;
+                                FP64 / FP32 reference-order kernels only */
 };
 
 /* fd_params.flags */
@@ -68,6 +71,8 @@ typedef struct fd_params {
   double gamma;        /* mobility */
   double psi_wall;     /* psi on solid cells */
   double outlet_coef;  /* 2/3 (fingering_periodic.py:317) or 1.5 (fingering.py:378) */
+  double force_x;      /* FD_VARIANT_PERIODIC_XY: body force per unit mass (Guo forcing, as mu grad psi) */
+  double force_y;
 } fd_params;
 
 /* Device pointers of the reference's Compute attributes (fingering_periodic.py:90-121). */

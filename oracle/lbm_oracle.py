@@ -49,6 +49,11 @@ class OracleParams:
     psi_wall: float         # psi written into solid cells (fingering_periodic.py:18)
     inlet_ux: np.ndarray    # (H,) inlet velocity per row (fingering_periodic.py:270-271 / fingering.py:299)
     outlet_coef: float      # 2/3 (fingering_periodic.py:317) or 1.5 (fingering.py:378)
+    # variant "periodic_xy" (an extension the reference does not have, so
+    # parity with it is unpinned): periodic in x too, no Zou-He, and a body
+    # force per unit mass added to mu grad psi in the velocity and the forcing
+    force_x: float = 0.0
+    force_y: float = 0.0
 
 
 def gaussian_inlet_profile(H: int, u0: float) -> np.ndarray:
@@ -73,8 +78,12 @@ def _padded_psi(psi, solid, prm: OracleParams):
     p[solid] = prm.psi_wall
     t = np.empty((H + 2, W + 2))
     t[1:-1, 1:-1] = p
-    t[1:-1, 0] = 1.0
-    t[1:-1, -1] = -1.0
+    if prm.variant == "periodic_xy":
+        t[1:-1, 0] = p[:, -1]
+        t[1:-1, -1] = p[:, 0]
+    else:
+        t[1:-1, 0] = 1.0
+        t[1:-1, -1] = -1.0
     if prm.variant == "walls":
         t[0, :] = prm.psi_wall
         t[-1, :] = prm.psi_wall
@@ -179,6 +188,10 @@ class OracleState:
             tx = tx + f[i][m] * EX[i]
         for i in range(9):
             ty = ty + f[i][m] * EY[i]
+        if self.prm.variant == "periodic_xy":
+            ux = ((tx + self.mu * self.npx[m] / 2) + self.rho * self.prm.force_x / 2) / self.rho
+            uy = ((ty + self.mu * self.npy[m] / 2) + self.rho * self.prm.force_y / 2) / self.rho
+            return ux, uy
         ux = (tx + self.mu * self.npx[m] / 2) / self.rho
         uy = (ty + self.mu * self.npy[m] / 2) / self.rho
         return ux, uy
@@ -211,8 +224,13 @@ class OracleState:
         ux, uy = self.ux, self.uy
         gx, gy = self.npx[m], self.npy[m]
         pref = self.mu * W9[:, None] * (1 - 1 / (2 * self.mix_tau))
-        return pref * (((EX[:, None] - ux) * 3 + EX[:, None] * eu * 9) * gx
-                       + ((EY[:, None] - uy) * 3 + EY[:, None] * eu * 9) * gy)
+        ax = (EX[:, None] - ux) * 3 + EX[:, None] * eu * 9
+        ay = (EY[:, None] - uy) * 3 + EY[:, None] * eu * 9
+        F = pref * (ax * gx + ay * gy)
+        if self.prm.variant == "periodic_xy":  # body force density rho b
+            prb = self.rho * W9[:, None] * (1 - 1 / (2 * self.mix_tau))
+            F = F + prb * (ax * self.prm.force_x + ay * self.prm.force_y)
+        return F
 
     # ------------------------------------------------------------------
     # one step: fingering_periodic.py:454-479 / fingering.py:558-585
@@ -255,6 +273,8 @@ class OracleState:
         return gx, gy, mu_plain(self.psi, self.np2, self.prm)
 
     def zou_he(self):
+        if self.prm.variant == "periodic_xy":
+            return
         gx, gy, mu = self.boundary_fields()
         if self.prm.variant == "walls":
             zou_he_inlet_walls(self.f, self.g, gx, gy, mu, self.prm)

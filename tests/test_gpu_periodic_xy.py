@@ -1,0 +1,89 @@
+"""The periodic-xy body-force extension on the GPU against the oracle's
+extension (tests/test_periodic_xy.py pins the oracle by exact physics; the
+reference has no such variant).  FP64 fused and per-function paths bit for
+bit, including BASELINE's small configuration at full length: 256 x 128,
+16 squares of side 10, tau 0.6 / 1.0, sigma 1e-3, 60 deg, g_x = 1e-5,
+2000 steps."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fingering_dynamics_gb300 import build
+    build.build()
+
+
+def _case(H, W, n, side, force, seed=3):
+    from fingering_dynamics_gb300 import geometry as geo
+    from fingering_dynamics_gb300.params import periodic_xy_params
+    from oracle.lbm_oracle import OracleParams, OracleState
+    prm = periodic_xy_params(H, W, force_x=force)
+    rects = geo.square_blocks(H, W, n, side, seed=seed)
+    g = geo.build_geometry(H, W, rects=rects, walls=False)
+    op = OracleParams(H=H, W=W, variant="periodic_xy", tau=prm.tau, eta_n=prm.eta_n, M=prm.M, a=prm.a,
+                      kappa=prm.kappa, gamma=prm.gamma, psi_wall=prm.psi_wall, inlet_ux=np.zeros(H),
+                      outlet_coef=prm.outlet_coef, force_x=prm.force_x, force_y=prm.force_y)
+    st = OracleState(op, g.solid, prm.initial_psi(g.solid))
+    return prm, g, st
+
+
+def _run_oracle(st, g, n):
+    for _ in range(n):
+        st.step(g.corner_list or None, None)
+
+
+@pytest.mark.parametrize("path", ["fused", "per_function"])
+def test_fp64_bitwise_small(path):
+    from fingering_dynamics_gb300.lattice import Lattice
+    prm, g, st = _case(48, 96, 4, 8, 1e-4)
+    lat = Lattice(prm, g, dtype="f64")
+    if path == "fused":
+        lat.step(40)
+    else:
+        lat.step_reference(40)
+    _run_oracle(st, g, 40)
+    got = lat.state()
+    assert np.array_equal(got["f"], st.f) and np.array_equal(got["g"], st.g)
+    assert np.array_equal(got["psi"], st.psi)
+
+
+def test_fp32_reference_order_close():
+    """FP32 with the reference's operand order: its known psi drift (the g_0
+    equilibrium formed as w0 * ((psi - c mu) / w0 + ...) rounds with a bias of
+    ~5e-8 per step) bounds the agreement, as for the reference variants."""
+    from fingering_dynamics_gb300.lattice import Lattice
+    prm, g, st = _case(48, 96, 4, 8, 1e-4)
+    lat = Lattice(prm, g, dtype="f32-exact")
+    lat.step(100)
+    _run_oracle(st, g, 100)
+    got = lat.state()
+    m = ~g.solid
+    assert np.abs(got["psi"][m] - st.psi[m]).max() <= 5e-5
+    assert np.abs(got["rho"][m] - st.rho).max() <= 1e-5
+
+
+def test_packed_kernels_reject_the_variant():
+    from fingering_dynamics_gb300 import _lib as L
+    from fingering_dynamics_gb300.lattice import Lattice
+    prm, g, _ = _case(48, 96, 4, 8, 1e-4)
+    lat = Lattice(prm, g, dtype="f32")
+    with pytest.raises(L.FDError, match="periodic-xy"):
+        lat.step(3)
+
+
+def test_small_configuration_2000_steps_bitwise():
+    from fingering_dynamics_gb300.lattice import Lattice
+    prm, g, st = _case(128, 256, 16, 10, 1e-5, seed=2024)
+    lat = Lattice(prm, g, dtype="f64")
+    lat.step(2000)
+    _run_oracle(st, g, 2000)
+    got = lat.state()
+    assert np.array_equal(got["f"], st.f) and np.array_equal(got["g"], st.g)
+    d = lat.diagnostics()
+    assert np.isfinite(d["mass_r"]) and 0.0 < d["saturation"] < 1.0
