@@ -417,7 +417,7 @@ def run_surrogate(args):
     with ClockSampler(0) as clk:
         torch.cuda.synchronize()
         e0.record(stream)
-        hist = train(net, train_f, steps=args.train_steps, batch=args.batch, lr=1e-3, seed=2,
+        hist = train(net, train_f, steps=args.train_steps, batch=args.batch, lr=1e-3, lr_end=5e-5, seed=2,
                      log_every=max(1, args.train_steps // 10))
         e1.record(stream)
         torch.cuda.synchronize()
@@ -453,6 +453,7 @@ def run_surrogate(args):
             "steps": args.train_steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "dtype": "bf16",
             "data": "synthetic (batched-LBM trajectories)",
             "config": {"workload": f"unet_{W}x{H}_batch{args.batch}", "widths": [32, 64, 128, 256],
+                       "optimizer": "AdamW, lr 1e-3 -> 5e-5 cosine, weight decay 1e-2",
                        "params": net.n_params, "members": M, "held_out_members": len(test_idx),
                        "train_members": len(train_idx), "frames_per_member": args.frames, "jump": jump,
                        "train_pairs": len(train_idx) * (args.frames - 1),

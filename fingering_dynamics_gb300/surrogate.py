@@ -329,19 +329,25 @@ def generate_trajectories(specs, n_frames: int, jump: int = 200, dtype: str = "f
 
 
 def train(net: UNet, frames: torch.Tensor, steps: int, batch: int = 32, lr: float = 1e-3, seed: int = 0,
-          log_every: int = 0):
+          log_every: int = 0, lr_end: float | None = None):
     """AdamW on random (frame k, frame k+1) pairs of `frames`
-    (members, n_frames, H, W, 4).  Returns the loss history (host floats)."""
+    (members, n_frames, H, W, 4); the learning rate follows a cosine from
+    `lr` to `lr_end` (constant if None).  Returns the loss history (host
+    floats)."""
     g = torch.Generator(device="cpu").manual_seed(seed)
     M, F = frames.shape[:2]
     hist = []
     for it in range(steps):
+        if lr_end is not None and steps > 1:
+            rate = lr_end + 0.5 * (lr - lr_end) * (1.0 + math.cos(math.pi * it / (steps - 1)))
+        else:
+            rate = lr
         mi = torch.randint(0, M, (batch,), generator=g)
         fi = torch.randint(0, F - 1, (batch,), generator=g)
         x = expand(frames[mi, fi])
         xn = expand(frames[mi, fi + 1])
         loss = net.loss_grad(x, xn)
-        net.adamw(lr=lr)
+        net.adamw(lr=rate)
         if log_every and (it % log_every == 0 or it == steps - 1):
             hist.append((it, float(loss.item())))
     return hist
