@@ -47,9 +47,6 @@ __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(smem_u32(p)));
 }
-__device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const void* p) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(smem_u32(p)));
-}
 __device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void* p) {
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
@@ -94,7 +91,7 @@ struct ConvCfg {
   static constexpr int VPR = BK / 8;                 // 16-byte vectors per row of a chunk
   static constexpr int A_VEC = BM * VPR, B_VEC = BN * VPR;
   static_assert(WM * WN == 4, "four warps");
-  static_assert(MT >= 1 && NT >= 1 && TM % 16 == 0 && TN % 8 == 0, "warp tile");
+  static_assert(MT >= 1 && NT % 2 == 0 && TM % 16 == 0 && TN % 16 == 0, "warp tile");
 };
 
 template <int BN, int BK, int WM, int WN>
@@ -111,36 +108,41 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ x
   const int co0 = blockIdx.y * BN;
   const int cchunks = Cin / BK, nk = 9 * cchunks;
 
-  // the pixels whose A vectors this thread copies (fixed over the K loop)
+  // the pixels whose A vectors this thread copies (fixed over the K loop):
+  // their address at the centre tap, their shared-memory slot and a 9-bit
+  // mask of the taps that fall inside the image
   constexpr int A_PER = (C::A_VEC + kThreads - 1) / kThreads;
-  int a_row[A_PER], a_sub[A_PER], a_n[A_PER], a_y[A_PER], a_x[A_PER];
+  const bf16* a_base[A_PER];
+  uint32_t a_valid[A_PER];
+  int a_soff[A_PER];
 #pragma unroll
   for (int i = 0; i < A_PER; ++i) {
     const int v = tid + i * kThreads;
-    a_row[i] = v / C::VPR;
-    a_sub[i] = v % C::VPR;
-    const long long p = m0 + a_row[i];
-    const bool ok = v < C::A_VEC && p < M;
-    const long long pp = ok ? p : 0;
-    a_n[i] = ok ? (int)(pp / ((long long)H * W)) : -1;
-    const int rem = (int)(pp % ((long long)H * W));
-    a_y[i] = rem / W;
-    a_x[i] = rem % W;
+    const int row = v / C::VPR, sub = v % C::VPR;
+    const long long p = m0 + row;
+    a_soff[i] = row * C::LDS + sub * 8;
+    a_base[i] = x;
+    a_valid[i] = 0u;
+    if (v < C::A_VEC && p < M) {
+      const int rem = (int)(p % ((long long)H * W));
+      const int yy = rem / W, xx = rem % W;
+      a_base[i] = x + p * Cin + sub * 8;
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const int ty = yy + t / 3 - 1, tx = xx + t % 3 - 1;
+        if (ty >= 0 && ty < H && tx >= 0 && tx < W) a_valid[i] |= 1u << t;
+      }
+    }
   }
 
   // K order: input-channel chunk major, the nine taps of a chunk back to back
   auto load_chunk = [&](int kc, int stage) {
     const int tap = kc % 9, ci0 = (kc / 9) * BK;
-    const int ky = tap / 3 - 1, kx = tap % 3 - 1;
+    const long long toff = ((long long)(tap / 3 - 1) * W + (tap % 3 - 1)) * Cin + ci0;
 #pragma unroll
     for (int i = 0; i < A_PER; ++i) {
-      const int v = tid + i * kThreads;
-      if (v < C::A_VEC) {
-        const int yy = a_y[i] + ky, xx = a_x[i] + kx;
-        const bool ok = a_n[i] >= 0 && yy >= 0 && yy < H && xx >= 0 && xx < W;
-        const bf16* src = ok ? x + (((long long)a_n[i] * H + yy) * W + xx) * Cin + ci0 + a_sub[i] * 8 : x;
-        cp16_l1(&As[stage][a_row[i] * C::LDS + a_sub[i] * 8], src, ok ? 16 : 0);
-      }
+      const bool ok = (a_valid[i] >> tap) & 1u;
+      if (tid + i * kThreads < C::A_VEC) cp16_l1(&As[stage][a_soff[i]], ok ? a_base[i] + toff : x, ok ? 16 : 0);
     }
     for (int v = tid; v < C::B_VEC; v += kThreads) {
       const int r = v / C::VPR, sub = v % C::VPR;
@@ -173,24 +175,16 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ x
         const int r = wm * C::TM + mt * 16 + (lane & 15);
         ldsm_x4(af[mt], &As[st][r * C::LDS + ks * 16 + (lane >> 4) * 8]);
       }
-      if constexpr (C::NT % 2 == 0) {
-        // two n8 fragments per ldmatrix: lanes 16..31 address the second
+      // two n8 fragments per ldmatrix: lanes 16..31 address the second
 #pragma unroll
-        for (int nt = 0; nt < C::NT; nt += 2) {
-          uint32_t r4[4];
-          const int r = wn * C::TN + nt * 8 + (lane & 7) + ((lane >> 4) << 3);
-          ldsm_x4(r4, &Bs[st][r * C::LDS + ks * 16 + ((lane >> 3) & 1) * 8]);
-          bfr[nt][0] = r4[0];
-          bfr[nt][1] = r4[1];
-          bfr[nt + 1][0] = r4[2];
-          bfr[nt + 1][1] = r4[3];
-        }
-      } else {
-#pragma unroll
-        for (int nt = 0; nt < C::NT; ++nt) {
-          const int r = wn * C::TN + nt * 8 + (lane & 7);
-          ldsm_x2(bfr[nt], &Bs[st][r * C::LDS + ks * 16 + ((lane >> 3) & 1) * 8]);
-        }
+      for (int nt = 0; nt < C::NT; nt += 2) {
+        uint32_t r4[4];
+        const int r = wn * C::TN + nt * 8 + (lane & 7) + ((lane >> 4) << 3);
+        ldsm_x4(r4, &Bs[st][r * C::LDS + ks * 16 + ((lane >> 3) & 1) * 8]);
+        bfr[nt][0] = r4[0];
+        bfr[nt][1] = r4[1];
+        bfr[nt + 1][0] = r4[2];
+        bfr[nt + 1][1] = r4[3];
       }
 #pragma unroll
       for (int mt = 0; mt < C::MT; ++mt)
@@ -276,26 +270,55 @@ __global__ void __launch_bounds__(kThreads) k_wgrad(const bf16* __restrict__ x, 
   const bool active = warp < C::WM * C::WN;
   const int wm = warp / C::WN, wn = warp % C::WN;
 
-  auto load_chunk = [&](long long pb, int st) {
-    for (int v = tid; v < C::AV; v += kThreads) {
-      const int r = v / (BM / 8), sub = v % (BM / 8);
-      const long long p = pb + r;
-      const bool ok = p < p1;
-      cp16(&As[st][r * C::LDA + sub * 8], ok ? dz + p * Cout + co0 + sub * 8 : dz, ok ? 16 : 0);
-    }
-    for (int v = tid; v < C::BV; v += kThreads) {
-      const int r = v / (BN / 8), sub = v % (BN / 8);
-      const long long p = pb + r;
-      bool ok = p < p1;
-      const bf16* src = x;
-      if (ok) {
-        const int n = (int)(p / ((long long)H * W));
-        const int rem = (int)(p % ((long long)H * W));
-        const int yy = rem / W + ky, xx = rem % W + kx;
-        ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
-        if (ok) src = x + (((long long)n * H + yy) * W + xx) * Cin + ci0 + sub * 8;
+  // Each thread copies fixed rows of every chunk: A rows are dz pixels, B
+  // rows x pixels shifted by the tap.  Their pixel index advances by BK per
+  // chunk; the (y, x) of the B rows is carried along without divisions.
+  constexpr int A_PER = (C::AV + kThreads - 1) / kThreads, B_PER = (C::BV + kThreads - 1) / kThreads;
+  long long a_p[A_PER], b_p[B_PER];
+  int b_y[B_PER], b_x[B_PER];
+#pragma unroll
+  for (int i = 0; i < A_PER; ++i) a_p[i] = p0 + (tid + i * kThreads) / (BM / 8);
+#pragma unroll
+  for (int i = 0; i < B_PER; ++i) {
+    b_p[i] = p0 + (tid + i * kThreads) / (BN / 8);
+    const int rem = (int)(b_p[i] % ((long long)H * W));
+    b_y[i] = rem / W;
+    b_x[i] = rem % W;
+  }
+  const long long toff = ((long long)ky * W + kx) * Cin + ci0;
+
+  auto load_chunk = [&](int st) {
+#pragma unroll
+    for (int i = 0; i < A_PER; ++i) {
+      const int v = tid + i * kThreads;
+      if (v < C::AV) {
+        const int r = v / (BM / 8), sub = v % (BM / 8);
+        const bool ok = a_p[i] < p1;
+        cp16(&As[st][r * C::LDA + sub * 8], ok ? dz + a_p[i] * Cout + co0 + sub * 8 : dz, ok ? 16 : 0);
       }
-      cp16(&Bs[st][r * C::LDB + sub * 8], src, ok ? 16 : 0);
+    }
+#pragma unroll
+    for (int i = 0; i < B_PER; ++i) {
+      const int v = tid + i * kThreads;
+      if (v < C::BV) {
+        const int r = v / (BN / 8), sub = v % (BN / 8);
+        const int yy = b_y[i] + ky, xx = b_x[i] + kx;
+        const bool ok = b_p[i] < p1 && yy >= 0 && yy < H && xx >= 0 && xx < W;
+        cp16(&Bs[st][r * C::LDB + sub * 8], ok ? x + b_p[i] * Cin + toff + sub * 8 : x, ok ? 16 : 0);
+      }
+    }
+  };
+  auto advance = [&]() {
+#pragma unroll
+    for (int i = 0; i < A_PER; ++i) a_p[i] += C::BK;
+#pragma unroll
+    for (int i = 0; i < B_PER; ++i) {
+      b_p[i] += C::BK;
+      b_x[i] += C::BK;
+      while (b_x[i] >= W) {
+        b_x[i] -= W;
+        if (++b_y[i] == H) b_y[i] = 0;
+      }
     }
   };
 
@@ -309,12 +332,15 @@ __global__ void __launch_bounds__(kThreads) k_wgrad(const bf16* __restrict__ x, 
 
   const long long nchunks = p1 > p0 ? (p1 - p0 + C::BK - 1) / C::BK : 0;
   if (nchunks > 0) {
-    load_chunk(p0, 0);
+    load_chunk(0);
     cp_commit();
   }
   for (long long kc = 0; kc < nchunks; ++kc) {
     const int st = (int)(kc & 1);
-    if (kc + 1 < nchunks) load_chunk(p0 + (kc + 1) * C::BK, st ^ 1);
+    if (kc + 1 < nchunks) {
+      advance();
+      load_chunk(st ^ 1);
+    }
     cp_commit();
     cp_wait<1>();
     __syncthreads();
