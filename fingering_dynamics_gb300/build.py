@@ -38,6 +38,7 @@ UNITS = {
     "fd_diag.cu": [],
     "fd_batch.cu": [],
     "sg_kernels.cu": [],
+    "sg_tcgen05.cu": [],
 }
 
 

@@ -1,0 +1,354 @@
+// 3x3 convolution (forward and data gradient) of the learned surrogate on the
+// fifth-generation tensor cores: tcgen05.mma with bfloat16 operands read from
+// shared memory through matrix descriptors and the FP32 accumulator in tensor
+// memory (TMEM).
+//
+// Implicit GEMM, M = pixels, N = output channels, K = 9 x input channels.  A
+// CTA of 128 threads owns 128 pixels x BN channels; the accumulator is 128
+// TMEM lanes x BN columns.  K advances in chunks of BK input channels of one
+// tap (the nine taps of a channel chunk back to back): all threads copy the
+// chunk's A (im2col rows) and B (weights) tiles into shared memory with
+// cp.async, in the canonical K-major layout without swizzle (core matrices
+// of 8 rows x 16 bytes; LBO = 128 B between the two core matrices of a K=16
+// slice, SBO = BK/8 x 128 B between 8-row groups), make them visible to the
+// async proxy, and one thread issues BK/16 MMAs (M=128, N=BN, K=16) and
+// commits them to the stage's mbarrier.  Two stages: a stage is refilled once
+// the MMAs that read it have completed.  The epilogue reads the accumulator
+// with tcgen05.ld (each warp its 32 lanes = 32 pixels), adds the bias,
+// applies GELU and stores bfloat16.
+//
+// Every mbarrier wait is bounded; a wait that gives up sets bit 0 of
+// g_sg_tc_error (read by sg_tc_status) and the kernel continues without
+// hanging; TMEM is always released.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fdsurrogate.h"
+#include "fd_host.h"
+
+namespace sg {
+
+__device__ unsigned int g_sg_tc_error = 0;
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+constexpr int kTcThreads = 128;
+constexpr int kTcBM = 128;
+constexpr unsigned kTcWaitLimit = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp16_l1(void* dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// bounded wait for phase `parity` of an mbarrier
+__device__ __forceinline__ void mbar_wait(uint64_t* bar, unsigned parity) {
+  const uint32_t a = smem_u32(bar);
+  for (unsigned it = 0; it < kTcWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return;
+  }
+  atomicOr(&g_sg_tc_error, 1u);
+}
+
+// shared-memory matrix descriptor: canonical K-major layout, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of this architecture
+  return d;                // base offset 0, layout "no swizzle" (bits 61..63 = 0)
+}
+
+// instruction descriptor of kind::f16: D FP32, A and B bfloat16, both K-major
+template <int M, int N>
+__device__ __forceinline__ constexpr uint32_t instr_desc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ float gelu_f(float z) {
+  const float u = 0.7978845608028654f * fmaf(0.044715f * z * z, z, z);
+  return 0.5f * z * (1.0f + tanhf(u));
+}
+
+// 32 lanes x 16 columns of 32-bit accumulators: thread t gets lane base+t, columns col..col+15
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int BN, int BK>
+struct TcCfg {
+  static constexpr int A_BYTES = kTcBM * BK * 2;  // 128 rows x BK bfloat16
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE = A_BYTES + B_BYTES;
+  static constexpr int SBO = (BK / 8) * 128;       // bytes between 8-row groups
+  static constexpr int LBO = 128;                  // bytes between the K=0..7 and K=8..15 core matrices
+  static constexpr int SMEM = 2 * STAGE + 64;      // two stages + barriers + TMEM address
+  static constexpr int COLS = BN < 32 ? 32 : BN;   // TMEM columns (power of two >= 32)
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "N of an M=128 MMA");
+  static_assert(BK % 16 == 0, "K chunk");
+};
+
+// byte offset of element (row, k) in a canonical K-major tile
+template <int BK>
+__device__ __forceinline__ uint32_t tile_off(int row, int k) {
+  return (uint32_t)((row & 7) * 16 + (row >> 3) * ((BK / 8) * 128) + (k >> 3) * 128 + (k & 7) * 2);
+}
+
+template <int BN, int BK>
+__global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const bf16* __restrict__ x, int N, int H, int W,
+                                                          int Cin, const bf16* __restrict__ w,
+                                                          const float* __restrict__ bias, int Cout, int act,
+                                                          bf16* __restrict__ z, bf16* __restrict__ y) {
+  using C = TcCfg<BN, BK>;
+  extern __shared__ __align__(1024) char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * C::STAGE);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 2 * C::STAGE + 32);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long M = (long long)N * H * W;
+  const long long m0 = (long long)blockIdx.x * kTcBM;
+  const int co0 = blockIdx.y * BN;
+  const int nk = 9 * (Cin / BK);
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(C::COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(&bars[0]);
+    mbar_init(&bars[1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  // this thread's A rows: pixel bases at the centre tap and tap-validity masks
+  constexpr int VPR = BK / 8;
+  constexpr int A_PER = kTcBM * VPR / kTcThreads;
+  static_assert(A_PER * kTcThreads == kTcBM * VPR, "A vectors per thread");
+  const bf16* a_base[A_PER];
+  uint32_t a_valid[A_PER], a_soff[A_PER];
+#pragma unroll
+  for (int i = 0; i < A_PER; ++i) {
+    const int v = tid + i * kTcThreads;
+    const int row = v / VPR, kv = v % VPR;
+    const long long p = m0 + row;
+    a_soff[i] = tile_off<BK>(row, kv * 8);
+    a_base[i] = x;
+    a_valid[i] = 0u;
+    if (p < M) {
+      const int rem = (int)(p % ((long long)H * W));
+      const int yy = rem / W, xx = rem % W;
+      a_base[i] = x + p * Cin + kv * 8;
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const int ty = yy + t / 3 - 1, tx = xx + t % 3 - 1;
+        if (ty >= 0 && ty < H && tx >= 0 && tx < W) a_valid[i] |= 1u << t;
+      }
+    }
+  }
+
+  auto load_chunk = [&](int kc, int st) {
+    char* As = smem + st * C::STAGE;
+    char* Bs = As + C::A_BYTES;
+    const int tap = kc % 9, ci0 = (kc / 9) * BK;
+    const long long toff = ((long long)(tap / 3 - 1) * W + (tap % 3 - 1)) * Cin + ci0;
+#pragma unroll
+    for (int i = 0; i < A_PER; ++i) {
+      const bool ok = (a_valid[i] >> tap) & 1u;
+      cp16_l1(As + a_soff[i], ok ? a_base[i] + toff : x, ok ? 16 : 0);
+    }
+    for (int v = tid; v < BN * VPR; v += kTcThreads) {
+      const int r = v / VPR, kv = v % VPR;
+      cp16(Bs + tile_off<BK>(r, kv * 8), w + ((long long)(co0 + r) * 9 + tap) * Cin + ci0 + kv * 8);
+    }
+  };
+
+  constexpr uint32_t idesc = instr_desc<kTcBM, BN>();
+  unsigned phase = 0;  // bit s: parity of the next completion of stage s
+  load_chunk(0, 0);
+  cp_commit();
+  for (int kc = 0; kc < nk; ++kc) {
+    const int st = kc & 1;
+    if (kc + 1 < nk) {
+      if (kc >= 1) {  // stage st^1 was read by the MMAs of chunk kc-1
+        mbar_wait(&bars[st ^ 1], (phase >> (st ^ 1)) & 1u);
+        phase ^= 1u << (st ^ 1);
+      }
+      load_chunk(kc + 1, st ^ 1);
+    }
+    cp_commit();
+    cp_wait<1>();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // cp.async data -> tensor core reads
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = smem_u32(smem + st * C::STAGE), b0 = a0 + C::A_BYTES;
+#pragma unroll
+      for (int s = 0; s < BK / 16; ++s) {
+        const uint64_t ad = smem_desc(a0 + s * 2 * C::LBO, C::LBO, C::SBO);
+        const uint64_t bd = smem_desc(b0 + s * 2 * C::LBO, C::LBO, C::SBO);
+        tc_mma(tmem, ad, bd, idesc, (kc > 0 || s > 0) ? 1u : 0u);
+      }
+      tc_commit(&bars[st]);
+    }
+  }
+  // the last commit of each stage that was used: wait for all MMAs
+  {
+    const int last = nk - 1;
+    const int st = last & 1;
+    mbar_wait(&bars[st], (phase >> st) & 1u);
+    phase ^= 1u << st;
+    if (nk >= 2) {
+      mbar_wait(&bars[st ^ 1], (phase >> (st ^ 1)) & 1u);
+      phase ^= 1u << (st ^ 1);
+    }
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  // epilogue: warp w holds pixels m0 + 32 w + lane
+  const long long p = m0 + warp * 32 + lane;
+#pragma unroll
+  for (int c0 = 0; c0 < BN; c0 += 16) {
+    float v[16];
+    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+    if (p < M) {
+      const int co = co0 + c0;
+      uint32_t zw[8], yw[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        float t0 = v[2 * i] + (bias ? bias[co + 2 * i] : 0.0f);
+        float t1 = v[2 * i + 1] + (bias ? bias[co + 2 * i + 1] : 0.0f);
+        const __nv_bfloat162 zp = __floats2bfloat162_rn(t0, t1);
+        zw[i] = *reinterpret_cast<const uint32_t*>(&zp);
+        if (act == SG_ACT_GELU) {
+          t0 = gelu_f(t0);
+          t1 = gelu_f(t1);
+        }
+        const __nv_bfloat162 yp = __floats2bfloat162_rn(t0, t1);
+        yw[i] = *reinterpret_cast<const uint32_t*>(&yp);
+      }
+      const size_t o = (size_t)p * Cout + co;
+      if (z) {
+        reinterpret_cast<uint4*>(z + o)[0] = make_uint4(zw[0], zw[1], zw[2], zw[3]);
+        reinterpret_cast<uint4*>(z + o)[1] = make_uint4(zw[4], zw[5], zw[6], zw[7]);
+      }
+      if (y) {
+        reinterpret_cast<uint4*>(y + o)[0] = make_uint4(yw[0], yw[1], yw[2], yw[3]);
+        reinterpret_cast<uint4*>(y + o)[1] = make_uint4(yw[4], yw[5], yw[6], yw[7]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::COLS) : "memory");
+  }
+}
+
+template <int BN, int BK>
+int launch_tc(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
+              bf16* z, bf16* y, cudaStream_t s) {
+  using C = TcCfg<BN, BK>;
+  auto kern = k_conv3x3_tc<BN, BK>;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) != cudaSuccess)
+      return fd::check_launch("sg_conv3x3_tc: shared-memory attribute");
+    attr = true;
+  }
+  const long long M = (long long)N * H * W;
+  dim3 grid((unsigned)((M + kTcBM - 1) / kTcBM), (unsigned)(Cout / BN));
+  kern<<<grid, kTcThreads, C::SMEM, s>>>(x, N, H, W, Cin, w, b, Cout, act, z, y);
+  return fd::check_launch("sg_conv3x3_tc");
+}
+
+template <int BK>
+int tc_bk(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act, bf16* z,
+          bf16* y, cudaStream_t s) {
+  if (Cout % 64 == 0) return launch_tc<64, BK>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  if (Cout % 32 == 0) return launch_tc<32, BK>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  return launch_tc<16, BK>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+}
+
+}  // namespace
+}  // namespace sg
+
+extern "C" {
+
+int sg_conv3x3_tc(const void* x, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout, int act,
+                  void* z, void* y, void* stream) {
+  FD_REQUIRE(x && w && (z || y) && N > 0 && H > 0 && W > 0, FD_ERR_ARG, "sg_conv3x3_tc: bad arguments");
+  FD_REQUIRE(Cin % 16 == 0 && Cout % 16 == 0 && Cin > 0 && Cout > 0, FD_ERR_SHAPE,
+             "sg_conv3x3_tc: channel counts must be positive multiples of 16 (got %d -> %d)", Cin, Cout);
+  FD_REQUIRE(act == SG_ACT_NONE || act == SG_ACT_GELU, FD_ERR_ARG, "sg_conv3x3_tc: activation %d", act);
+  FD_REQUIRE(((uintptr_t)x | (uintptr_t)w | (uintptr_t)z | (uintptr_t)y) % 16 == 0, FD_ERR_ARG,
+             "sg_conv3x3_tc: tensors must be 16-byte aligned");
+  using sg::bf16;
+  cudaStream_t s = fd::as_stream(stream);
+  const bf16 *xb = (const bf16*)x, *wb = (const bf16*)w;
+  if (Cin % 64 == 0) return sg::tc_bk<64>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
+  if (Cin % 32 == 0) return sg::tc_bk<32>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
+  return sg::tc_bk<16>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
+}
+
+int sg_tc_status(unsigned* out, int clear) {
+  FD_REQUIRE(out != nullptr, FD_ERR_ARG, "sg_tc_status: NULL pointer");
+  if (cudaMemcpyFromSymbol(out, sg::g_sg_tc_error, sizeof(unsigned)) != cudaSuccess)
+    return fd::check_launch("sg_tc_status");
+  if (clear) {
+    const unsigned zero = 0;
+    if (cudaMemcpyToSymbol(sg::g_sg_tc_error, &zero, sizeof(unsigned)) != cudaSuccess)
+      return fd::check_launch("sg_tc_status");
+  }
+  return FD_OK;
+}
+
+}  // extern "C"

@@ -31,6 +31,14 @@ enum sg_act { SG_ACT_NONE = 0, SG_ACT_GELU = 1 };
 int sg_conv3x3(const void* x, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout, int act,
                void* z, void* y, void* stream);
 
+/* sg_conv3x3 on the fifth-generation tensor cores (tcgen05.mma, operands in
+ * shared memory through matrix descriptors, accumulator in tensor memory);
+ * same arguments and results.  sg_tc_status reads (and optionally clears) its
+ * device error word: bit 0 = an mbarrier wait gave up. */
+int sg_conv3x3_tc(const void* x, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout, int act,
+                  void* z, void* y, void* stream);
+int sg_tc_status(unsigned* out, int clear);
+
 /* wt[ci][ky][kx][co] = w[co][2-ky][2-kx][ci]: the weights of the data-gradient
  * convolution (dx = sg_conv3x3(dz, wt)). */
 int sg_flip_weights(const void* w, int Cin, int Cout, void* wt, void* stream);

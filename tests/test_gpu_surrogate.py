@@ -168,3 +168,39 @@ def test_rollout_judge_accepts_or_falls_back():
     assert bool(torch.isfinite(lat.psi).all())
     for r in recs:
         assert r["accepted"] == (abs(r["sat_lbm"] - r["sat_surrogate"]) <= 0.02 * r["sat_lbm"])
+
+
+def _tc_status(clear=True):
+    import ctypes as C
+    from fingering_dynamics_gb300 import _lib as L
+    v = C.c_uint(0)
+    L.call("sg_tc_status", C.byref(v), int(clear))
+    return v.value
+
+
+@pytest.mark.parametrize("n,h,w,cin,cout,act", [(1, 8, 16, 16, 16, 0), (2, 8, 40, 32, 32, 1), (2, 16, 24, 64, 64, 1),
+                                                (1, 8, 16, 96, 32, 0), (2, 8, 32, 256, 128, 1)])
+def test_tcgen05_conv_matches_oracle(n, h, w, cin, cout, act):
+    """The tcgen05 / TMEM convolution against the oracle and against the
+    warp-level tensor-core kernel (same inputs; both accumulate in FP32)."""
+    rng = np.random.default_rng(cin * 7 + cout)
+    xh, x = _bf(rng.normal(size=(n, h, w, cin)))
+    wh, wt = _bf(rng.normal(0, 0.2, size=(cout, 3, 3, cin)))
+    b = rng.normal(0, 0.1, cout).astype(np.float32)
+    bd = torch.from_numpy(b).cuda()
+    outs = {}
+    for name in ("sg_conv3x3_tc", "sg_conv3x3"):
+        z = torch.zeros((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
+        y = torch.zeros_like(z)
+        _call(name, _p(x), n, h, w, cin, _p(wt), _p(bd), cout, act, _p(z), _p(y), None)
+        torch.cuda.synchronize()
+        outs[name] = (z.float().cpu().numpy(), y.float().cpu().numpy())
+    assert _tc_status() == 0
+    zr = U.conv3x3(xh, wh, b.astype(np.float64))
+    yr = U.gelu(zr) if act else zr
+    scale = np.abs(zr).max()
+    ztc, ytc = outs["sg_conv3x3_tc"]
+    assert np.abs(ztc - zr).max() <= 1e-2 * scale
+    assert np.abs(ytc - yr).max() <= 1e-2 * scale
+    # the two tensor-core paths round their FP32 sums to the same bfloat16 almost everywhere
+    assert np.mean(ztc != outs["sg_conv3x3"][0]) < 0.02
