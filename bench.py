@@ -410,7 +410,7 @@ def run_surrogate(args):
     train_idx = [i for i in range(M - held) if fin[i]]
     test_idx = [i for i in range(M - held, M) if fin[i]]
     train_f, test_f = frames[train_idx], frames[test_idx]
-    net = UNet((32, 64, 128, 256), seed=0)
+    net = UNet((32, 64, 128, 256), seed=0, conv=args.conv)
     train(net, train_f, steps=args.warmup, batch=args.batch, seed=1)
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -453,6 +453,8 @@ def run_surrogate(args):
             "steps": args.train_steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "dtype": "bf16",
             "data": "synthetic (batched-LBM trajectories)",
             "config": {"workload": f"unet_{W}x{H}_batch{args.batch}", "widths": [32, 64, 128, 256],
+                       "conv_kernel": args.conv,
+                       "conv_choice": {"x".join(map(str, k)): v for k, v in net.conv_choice.items()},
                        "optimizer": "AdamW, lr 1e-3 -> 5e-5 cosine, weight decay 1e-2",
                        "params": net.n_params, "members": M, "held_out_members": len(test_idx),
                        "train_members": len(train_idx), "frames_per_member": args.frames, "jump": jump,
@@ -469,6 +471,45 @@ def run_surrogate(args):
     return 0
 
 
+def run_convs(args):
+    """Every convolution shape of the surrogate's training step (forward and
+    data gradient, batch `--batch` at 512 x 256): the warp-level and the
+    tcgen05 kernel timed with CUDA events, one JSON line per shape."""
+    import ctypes as C
+    import torch
+    from fingering_dynamics_gb300 import _lib as L
+    from fingering_dynamics_gb300 import build
+    build.build()
+
+    def p(t):
+        return C.c_void_p(t.data_ptr())
+    N = args.batch
+    shapes = [(256, 512, 16, 32), (256, 512, 32, 32), (128, 256, 32, 64), (128, 256, 64, 64), (64, 128, 64, 128),
+              (64, 128, 128, 128), (32, 64, 128, 256), (32, 64, 256, 256), (64, 128, 384, 128),
+              (128, 256, 192, 64), (256, 512, 96, 32), (256, 512, 32, 16), (256, 512, 32, 96),
+              (128, 256, 64, 192), (64, 128, 128, 384), (32, 64, 256, 128)]
+    for (H, W, ci, co) in shapes:
+        x = torch.randn(N, H, W, ci, device="cuda").to(torch.bfloat16)
+        w = (0.1 * torch.randn(co, 3, 3, ci, device="cuda")).to(torch.bfloat16)
+        y = torch.empty(N, H, W, co, device="cuda", dtype=torch.bfloat16)
+        z = torch.empty_like(y)
+        fl = 2.0 * 9 * ci * co * N * H * W
+        line = {"metric": "conv3x3 throughput", "unit": "TFLOP/s", "shape": [N, H, W, ci, co]}
+        for fn, key in (("sg_conv3x3", "mma"), ("sg_conv3x3_tc", "tcgen05")):
+            for _ in range(args.warmup):
+                L.call(fn, p(x), N, H, W, ci, p(w), None, co, 1, p(z), p(y), None)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                L.call(fn, p(x), N, H, W, ci, p(w), None, co, 1, p(z), p(y), None)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            line[key] = {"us": round(ms * 1e3, 1), "tflops": round(fl / ms / 1e9, 1)}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -481,7 +522,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end measurement")
     ap.add_argument("--H", type=int, default=H_FULL, help="lattice rows (default: the 4096 x 2048 workload)")
     ap.add_argument("--W", type=int, default=W_FULL, help="lattice columns")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "precision", "surrogate"],
+    ap.add_argument("--workload", default="single",
+                    choices=["single", "ensemble", "precision", "surrogate", "surrogate-convs"],
                     help="single 4096 x 2048 lattice (default), the batched ensemble, or the error study of "
                          "reduced-precision storage against the FP64 path (1024 x 256, --steps iterations)")
     ap.add_argument("--rounding", default="stochastic", choices=["stochastic", "nearest"],
@@ -492,6 +534,8 @@ def main():
     ap.add_argument("--frames", type=int, default=41, help="surrogate: frames per member (one per 200 iterations)")
     ap.add_argument("--train-steps", type=int, default=1000, help="surrogate: timed AdamW steps")
     ap.add_argument("--batch", type=int, default=32, help="surrogate: training batch")
+    ap.add_argument("--conv", default="auto", choices=["auto", "mma", "tcgen05"],
+                    help="surrogate: forward / data-gradient convolution kernel (auto: the faster per shape)")
     ap.add_argument("--family", default="stable", choices=["stable", "spec"],
                     help="ensemble parameter family (spec: the configuration's literal ranges)")
     args = ap.parse_args()
@@ -505,6 +549,8 @@ def main():
         return run_precision(args)
     if args.workload == "surrogate":
         return run_surrogate(args)
+    if args.workload == "surrogate-convs":
+        return run_convs(args)
     return run_ours(args)
 
 

@@ -12,8 +12,9 @@
 // of 8 rows x 16 bytes; LBO = 128 B between the two core matrices of a K=16
 // slice, SBO = BK/8 x 128 B between 8-row groups), make them visible to the
 // async proxy, and one thread issues BK/16 MMAs (M=128, N=BN, K=16) and
-// commits them to the stage's mbarrier.  Two stages: a stage is refilled once
-// the MMAs that read it have completed.  The epilogue reads the accumulator
+// commits them to the stage's mbarrier.  Four stages: three chunks are in
+// flight while one is multiplied, and a stage is refilled once the MMAs that
+// read it have completed.  The epilogue reads the accumulator
 // with tcgen05.ld (each warp its 32 lanes = 32 pixels), adds the bias,
 // applies GELU and stores bfloat16.
 //
@@ -119,14 +120,17 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+constexpr int kTcStages = 4;
+
 template <int BN, int BK>
 struct TcCfg {
+  static constexpr int S = kTcStages;
   static constexpr int A_BYTES = kTcBM * BK * 2;  // 128 rows x BK bfloat16
   static constexpr int B_BYTES = BN * BK * 2;
   static constexpr int STAGE = A_BYTES + B_BYTES;
   static constexpr int SBO = (BK / 8) * 128;       // bytes between 8-row groups
   static constexpr int LBO = 128;                  // bytes between the K=0..7 and K=8..15 core matrices
-  static constexpr int SMEM = 2 * STAGE + 64;      // two stages + barriers + TMEM address
+  static constexpr int SMEM = S * STAGE + 128;     // stages + barriers + TMEM address
   static constexpr int COLS = BN < 32 ? 32 : BN;   // TMEM columns (power of two >= 32)
   static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "N of an M=128 MMA");
   static_assert(BK % 16 == 0, "K chunk");
@@ -145,8 +149,8 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const bf16* __restric
                                                           bf16* __restrict__ z, bf16* __restrict__ y) {
   using C = TcCfg<BN, BK>;
   extern __shared__ __align__(1024) char smem[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * C::STAGE);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 2 * C::STAGE + 32);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::S * C::STAGE);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + C::S * C::STAGE + 8 * C::S);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long M = (long long)N * H * W;
   const long long m0 = (long long)blockIdx.x * kTcBM;
@@ -160,8 +164,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const bf16* __restric
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init(&bars[0]);
-    mbar_init(&bars[1]);
+    for (int i = 0; i < C::S; ++i) mbar_init(&bars[i]);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -213,19 +216,25 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const bf16* __restric
 
   constexpr uint32_t idesc = instr_desc<kTcBM, BN>();
   unsigned phase = 0;  // bit s: parity of the next completion of stage s
-  load_chunk(0, 0);
-  cp_commit();
+  auto wait_stage = [&](int s) {
+    mbar_wait(&bars[s], (phase >> s) & 1u);
+    phase ^= 1u << s;
+  };
+  // prologue: chunks 0 .. S-2 in flight
+#pragma unroll
+  for (int i = 0; i < C::S - 1; ++i) {
+    if (i < nk) load_chunk(i, i);
+    cp_commit();
+  }
   for (int kc = 0; kc < nk; ++kc) {
-    const int st = kc & 1;
-    if (kc + 1 < nk) {
-      if (kc >= 1) {  // stage st^1 was read by the MMAs of chunk kc-1
-        mbar_wait(&bars[st ^ 1], (phase >> (st ^ 1)) & 1u);
-        phase ^= 1u << (st ^ 1);
-      }
-      load_chunk(kc + 1, st ^ 1);
+    const int st = kc % C::S;
+    const int nxt = kc + C::S - 1;  // refills the stage chunk kc-1 used
+    if (nxt < nk) {
+      if (kc >= 1) wait_stage((kc - 1) % C::S);
+      load_chunk(nxt, nxt % C::S);
     }
     cp_commit();
-    cp_wait<1>();
+    cp_wait<C::S - 1>();  // chunk kc has landed
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // cp.async data -> tensor core reads
     __syncthreads();
     if (tid == 0) {
@@ -240,17 +249,8 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const bf16* __restric
       tc_commit(&bars[st]);
     }
   }
-  // the last commit of each stage that was used: wait for all MMAs
-  {
-    const int last = nk - 1;
-    const int st = last & 1;
-    mbar_wait(&bars[st], (phase >> st) & 1u);
-    phase ^= 1u << st;
-    if (nk >= 2) {
-      mbar_wait(&bars[st ^ 1], (phase >> (st ^ 1)) & 1u);
-      phase ^= 1u << (st ^ 1);
-    }
-  }
+  // the commits not waited for in the loop: chunks max(0, nk-S) .. nk-1
+  for (int c = (nk > C::S ? nk - C::S : 0); c < nk; ++c) wait_stage(c % C::S);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   // epilogue: warp w holds pixels m0 + 32 w + lane
@@ -291,6 +291,191 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const bf16* __restric
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::COLS) : "memory");
   }
+}
+
+// ---------------------------------------------------------------------------
+// Halo-tile variant for images whose width is a multiple of 128: a CTA owns
+// 128 pixels of one image row.  Per input-channel chunk it copies the three
+// input rows y-1, y, y+1 over 130 pixels (x0-1 .. x0+128, zeros outside the
+// image) once, and the weights of all nine taps; each tap's A operand is the
+// 128-row window that starts (1 + kx) pixels into row block ky + 1.  The
+// window can start on any pixel because the rows of a block are 16 bytes
+// apart with no gap between 8-row groups (SBO = 128 B) and the two K halves
+// of a 16-wide slice sit a whole block column apart (LBO = 130 x 16 B).  The
+// input is read once per tile instead of nine times.
+// ---------------------------------------------------------------------------
+constexpr int kHaloPx = kTcBM + 2;
+
+template <int BN, int BK, int R>
+struct HaloCfg {
+  static constexpr int LBO_A = kHaloPx * 16;            // between the K-slices of a row block
+  static constexpr int BLK = (BK / 8) * LBO_A;          // one input row block
+  static constexpr int A_BYTES = (R + 2) * BLK;         // input rows y0-1 .. y0+R
+  static constexpr int TB = BN * BK * 2;                // one tap's weights (canonical K-major)
+  static constexpr int B_BYTES = 9 * TB;
+  static constexpr int STAGE = (A_BYTES + B_BYTES + 127) / 128 * 128;
+  static constexpr int SMEM = 2 * STAGE + 128;
+  static constexpr int NCOL = R * BN;                   // R accumulators of BN columns
+  static constexpr int COLS = NCOL <= 32 ? 32 : (NCOL <= 64 ? 64 : (NCOL <= 128 ? 128 : (NCOL <= 256 ? 256 : 512)));
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256 && BK % 16 == 0 && NCOL <= 512, "tile");
+};
+
+template <int BN, int BK, int R>
+__global__ void __launch_bounds__(kTcThreads) k_conv3x3_tch(const bf16* __restrict__ x, int N, int H, int W,
+                                                           int Cin, const bf16* __restrict__ w,
+                                                           const float* __restrict__ bias, int Cout, int act,
+                                                           bf16* __restrict__ z, bf16* __restrict__ y) {
+  using C = HaloCfg<BN, BK, R>;
+  extern __shared__ __align__(1024) char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * C::STAGE);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 2 * C::STAGE + 32);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tiles_x = W / kTcBM;
+  const int tx = blockIdx.x % tiles_x, rblk = blockIdx.x / tiles_x;  // block of R image rows
+  const int row = rblk * R;                                          // first row = n * H + yy (H % R == 0)
+  const int yy = row % H;
+  const int x0 = tx * kTcBM;
+  const int co0 = blockIdx.y * BN;
+  const int nk = Cin / BK;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(C::COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(&bars[0]);
+    mbar_init(&bars[1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  constexpr int VPR = BK / 8;  // 16-byte vectors per pixel of a chunk
+  auto load_chunk = [&](int kc, int st) {
+    char* As = smem + st * C::STAGE;
+    char* Bs = As + C::A_BYTES;
+    const int ci0 = kc * BK;
+    for (int v = tid; v < (R + 2) * kHaloPx * VPR; v += kTcThreads) {
+      const int kv = v % VPR, px = (v / VPR) % kHaloPx, rb = v / (VPR * kHaloPx);
+      const int sy = yy + rb - 1, sx = x0 + px - 1;
+      const bool ok = sy >= 0 && sy < H && sx >= 0 && sx < W;
+      const bf16* src = ok ? x + ((long long)(row + rb - 1) * W + sx) * Cin + ci0 + kv * 8 : x;
+      cp16_l1(As + rb * C::BLK + kv * C::LBO_A + px * 16, src, ok ? 16 : 0);
+    }
+    for (int v = tid; v < 9 * BN * VPR; v += kTcThreads) {
+      const int kv = v % VPR, r = (v / VPR) % BN, tap = v / (VPR * BN);
+      cp16(Bs + tap * C::TB + tile_off<BK>(r, kv * 8), w + ((long long)(co0 + r) * 9 + tap) * Cin + ci0 + kv * 8);
+    }
+  };
+
+  constexpr uint32_t idesc = instr_desc<kTcBM, BN>();
+  unsigned phase = 0;
+  auto wait_stage = [&](int s) {
+    mbar_wait(&bars[s], (phase >> s) & 1u);
+    phase ^= 1u << s;
+  };
+  load_chunk(0, 0);
+  cp_commit();
+  for (int kc = 0; kc < nk; ++kc) {
+    const int st = kc & 1;
+    if (kc + 1 < nk) {
+      if (kc >= 1) wait_stage(st ^ 1);  // stage st^1 was read by the MMAs of chunk kc-1
+      load_chunk(kc + 1, st ^ 1);
+    }
+    cp_commit();
+    cp_wait<1>();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = smem_u32(smem + st * C::STAGE), b0 = a0 + C::A_BYTES;
+#pragma unroll
+      for (int tap = 0; tap < 9; ++tap) {
+        const int ky = tap / 3, kx = tap % 3;  // row block r + ky, window start kx (= 1 + (kx - 1))
+#pragma unroll
+        for (int s = 0; s < BK / 16; ++s) {
+          const uint64_t bd = smem_desc(b0 + tap * C::TB + s * 256, 128, (BK / 8) * 128);
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const uint64_t ad = smem_desc(a0 + (r + ky) * C::BLK + 2 * s * C::LBO_A + kx * 16, C::LBO_A, 128);
+            tc_mma(tmem + (uint32_t)(r * BN), ad, bd, idesc, (kc > 0 || tap > 0 || s > 0) ? 1u : 0u);
+          }
+        }
+      }
+      tc_commit(&bars[st]);
+    }
+  }
+  for (int c = (nk > 2 ? nk - 2 : 0); c < nk; ++c) wait_stage(c & 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+#pragma unroll 1
+  for (int r = 0; r < R; ++r) {
+    const long long p = ((long long)(row + r) * W + x0) + warp * 32 + lane;
+#pragma unroll
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(r * BN + c0), v);
+      const int co = co0 + c0;
+      uint32_t zw[8], yw[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        float t0 = v[2 * i] + (bias ? bias[co + 2 * i] : 0.0f);
+        float t1 = v[2 * i + 1] + (bias ? bias[co + 2 * i + 1] : 0.0f);
+        const __nv_bfloat162 zp = __floats2bfloat162_rn(t0, t1);
+        zw[i] = *reinterpret_cast<const uint32_t*>(&zp);
+        if (act == SG_ACT_GELU) {
+          t0 = gelu_f(t0);
+          t1 = gelu_f(t1);
+        }
+        const __nv_bfloat162 yp = __floats2bfloat162_rn(t0, t1);
+        yw[i] = *reinterpret_cast<const uint32_t*>(&yp);
+      }
+      const size_t o = (size_t)p * Cout + co;
+      if (z) {
+        reinterpret_cast<uint4*>(z + o)[0] = make_uint4(zw[0], zw[1], zw[2], zw[3]);
+        reinterpret_cast<uint4*>(z + o)[1] = make_uint4(zw[4], zw[5], zw[6], zw[7]);
+      }
+      if (y) {
+        reinterpret_cast<uint4*>(y + o)[0] = make_uint4(yw[0], yw[1], yw[2], yw[3]);
+        reinterpret_cast<uint4*>(y + o)[1] = make_uint4(yw[4], yw[5], yw[6], yw[7]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::COLS) : "memory");
+  }
+}
+
+template <int BN, int BK, int R>
+int launch_tch_r(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
+                 bf16* z, bf16* y, cudaStream_t s) {
+  using C = HaloCfg<BN, BK, R>;
+  auto kern = k_conv3x3_tch<BN, BK, R>;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) != cudaSuccess)
+      return fd::check_launch("sg_conv3x3_tc: shared-memory attribute");
+    attr = true;
+  }
+  dim3 grid((unsigned)((long long)N * (H / R) * (W / kTcBM)), (unsigned)(Cout / BN));
+  kern<<<grid, kTcThreads, C::SMEM, s>>>(x, N, H, W, Cin, w, b, Cout, act, z, y);
+  return fd::check_launch("sg_conv3x3_tc");
+}
+
+// rows per CTA: four where the height allows (the weights of a chunk then
+// serve 512 pixels), else two or one
+template <int BN, int BK>
+int launch_tch(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
+               bf16* z, bf16* y, cudaStream_t s) {
+  if (H % 4 == 0) return launch_tch_r<BN, BK, 4>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  if (H % 2 == 0) return launch_tch_r<BN, BK, 2>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  return launch_tch_r<BN, BK, 1>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
 }
 
 template <int BN, int BK>
@@ -334,6 +519,17 @@ int sg_conv3x3_tc(const void* x, int N, int H, int W, int Cin, const void* w, co
   using sg::bf16;
   cudaStream_t s = fd::as_stream(stream);
   const bf16 *xb = (const bf16*)x, *wb = (const bf16*)w;
+  if (W % sg::kTcBM == 0) {  // halo tiles: the input is read once per tile
+    bf16 *zb = (bf16*)z, *yb = (bf16*)y;
+    if (Cin % 32 == 0) {
+      if (Cout % 64 == 0) return sg::launch_tch<64, 32>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+      if (Cout % 32 == 0) return sg::launch_tch<32, 32>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+      return sg::launch_tch<16, 32>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+    }
+    if (Cout % 64 == 0) return sg::launch_tch<64, 16>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+    if (Cout % 32 == 0) return sg::launch_tch<32, 16>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+    return sg::launch_tch<16, 16>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+  }
   if (Cin % 64 == 0) return sg::tc_bk<64>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
   if (Cin % 32 == 0) return sg::tc_bk<32>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
   return sg::tc_bk<16>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);

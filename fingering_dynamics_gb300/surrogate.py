@@ -1,8 +1,10 @@
 """Learned surrogate: a convolutional U-Net that advances (psi, u_x, u_y) by a
 fixed number of lattice steps (a "jump") given the solid mask, trained on
 trajectories of the batched LBM with this package's own CUDA kernels
-(include/fdsurrogate.h: tensor-core implicit-GEMM convolutions forward, data
-and weight gradients, and the training elementwise kernels), and a rollout
+(include/fdsurrogate.h: tensor-core implicit-GEMM convolutions, forward and
+data gradient on tcgen05 with the accumulator in tensor memory or on
+warp-level MMA, whichever is faster for the shape, weight gradient on
+warp-level MMA, and the training elementwise kernels), and a rollout
 driver that uses the plain LBM as its judge and fallback.
 
 The reference has no learned component.  Network (widths c1..c4, 3x3 convs,
@@ -81,7 +83,17 @@ class UNet:
     """The network, its FP32 master weights, bfloat16 copies, AdamW moments and
     activation buffers (allocated per batch shape)."""
 
-    def __init__(self, widths=(32, 64, 128, 256), seed: int = 0, device="cuda", params: dict | None = None):
+    def __init__(self, widths=(32, 64, 128, 256), seed: int = 0, device="cuda", params: dict | None = None,
+                 conv: str = "auto"):
+        """``conv`` selects the forward and data-gradient convolution kernel:
+        "tcgen05" (fifth-generation tensor cores, accumulator in tensor
+        memory), "mma" (warp-level tensor-core instructions) or "auto" (both
+        timed once per convolution shape at first use, the faster kept); the
+        weight gradient always uses the warp-level kernel."""
+        if conv not in ("tcgen05", "mma", "auto"):
+            raise ValueError("conv must be 'tcgen05', 'mma' or 'auto'")
+        self.conv = conv
+        self.conv_choice = {}  # (N, H, W, Cin, Cout) -> kernel name, filled by "auto"
         self.widths = tuple(widths)
         self.shapes = layer_shapes(self.widths)
         self.device = torch.device(device)
@@ -164,12 +176,38 @@ class UNet:
         self._buf[key] = B
         return B
 
+    _KERNELS = {"mma": "sg_conv3x3", "tcgen05": "sg_conv3x3_tc"}
+
+    def _run_conv(self, x, N, h, w, ci, wt, bias, co, act, z, y):
+        """One 3x3 convolution with the kernel chosen for its shape."""
+        key = (N, h, w, ci, co)
+        args = (_p(x), N, h, w, ci, _p(wt), _p(bias), co, act, _p(z), _p(y), _s())
+        if self.conv != "auto":
+            fn = self._KERNELS[self.conv]
+        elif key in self.conv_choice:
+            fn = self.conv_choice[key]
+        else:  # time both once on the real operands; the last call's result stands
+            best = None
+            for fn in self._KERNELS.values():
+                L.call(fn, *args)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(2):
+                    L.call(fn, *args)
+                e1.record()
+                e1.synchronize()
+                t = e0.elapsed_time(e1)
+                if best is None or t < best[0]:
+                    best = (t, fn)
+            fn = self.conv_choice[key] = best[1]
+        L.call(fn, *args)
+
     def _conv(self, name, x, B, act=True):
         ci, co = self.shapes[name]
         N, h, w, c = x.shape
         assert c == ci, (name, c, ci)
-        L.call("sg_conv3x3", _p(x), N, h, w, ci, _p(self.w16[name]), _p(self.b[name]), co,
-               1 if act else 0, _p(B["z." + name]) if act else None, _p(B["y." + name]), _s())
+        self._run_conv(x, N, h, w, ci, self.w16[name], self.b[name], co, 1 if act else 0,
+                       B["z." + name] if act else None, B["y." + name])
         return B["y." + name]
 
     def forward(self, x: torch.Tensor) -> torch.Tensor:
@@ -224,7 +262,7 @@ class UNet:
         if not need_dx:
             return None
         dx = B["dx." + name]
-        L.call("sg_conv3x3", _p(dz), N, h, w, co, _p(self.wt16[name]), None, ci, 0, None, _p(dx), s)
+        self._run_conv(dz, N, h, w, co, self.wt16[name], None, ci, 0, None, dx)
         return dx
 
     def _gelu_back(self, name, dy, B):

@@ -179,7 +179,11 @@ def _tc_status(clear=True):
 
 
 @pytest.mark.parametrize("n,h,w,cin,cout,act", [(1, 8, 16, 16, 16, 0), (2, 8, 40, 32, 32, 1), (2, 16, 24, 64, 64, 1),
-                                                (1, 8, 16, 96, 32, 0), (2, 8, 32, 256, 128, 1)])
+                                                (1, 8, 16, 96, 32, 0), (2, 8, 32, 256, 128, 1),
+                                                # widths that are multiples of 128: the halo-tile kernel
+                                                (1, 4, 128, 16, 32, 1), (2, 3, 128, 32, 64, 0),
+                                                (1, 2, 256, 64, 64, 1), (1, 3, 128, 96, 32, 1),
+                                                (1, 2, 128, 16, 16, 0)])
 def test_tcgen05_conv_matches_oracle(n, h, w, cin, cout, act):
     """The tcgen05 / TMEM convolution against the oracle and against the
     warp-level tensor-core kernel (same inputs; both accumulate in FP32)."""
