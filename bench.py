@@ -205,6 +205,32 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# replicas across ranks (host logic, any torch.distributed backend)
+# ---------------------------------------------------------------------------
+def replica_seed(rank: int) -> int:
+    """Geometry seed of rank `rank`'s lattice: every rank runs its own
+    instance of the workload (replicas, no data-path collective)."""
+    return 2024 + rank
+
+
+def max_over_ranks(values, device="cpu"):
+    """Element-wise max of `values` over all ranks of the default process
+    group (the slowest rank bounds the job's time); identity without one."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def job_mlups(world: int, cells: int, steps: int, ms_total: float) -> float:
+    """Whole-job lattice updates per second: all ranks' cells over the
+    slowest rank's time."""
+    return world * cells * steps / (ms_total / 1e3) / 1e6
+
+
+# ---------------------------------------------------------------------------
 # GPU timing
 # ---------------------------------------------------------------------------
 def run_ours(args):
@@ -225,7 +251,7 @@ def run_ours(args):
     from fingering_dynamics_gb300 import build
     from fingering_dynamics_gb300.lattice import Lattice
     build.build()
-    prm, g = workload(args.H, args.W, seed=2024 + rank)
+    prm, g = workload(args.H, args.W, seed=replica_seed(rank))
     lat = Lattice(prm, g, dtype=args.dtype, device=f"cuda:{local}", rounding=args.rounding)
     H, W = prm.H, prm.W
     lat.enter_fused()
@@ -272,15 +298,12 @@ def run_ours(args):
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
 
-    t = torch.tensor([ms_total, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_total, e2e_s = float(t[0]), float(t[1])
+    ms_total, e2e_s = max_over_ranks([ms_total, e2e_s], device=f"cuda:{local}")
     if rank == 0:
 
         ms_step = ms_total / args.steps
         cells = H * W
-        mlups = world * cells * args.steps / (ms_total / 1e3) / 1e6
+        mlups = job_mlups(world, cells, args.steps, ms_total)
         alg_bytes = BYTES_PER_LU[args.dtype] * cells
         achieved = alg_bytes / (ms_step / 1e3) / 1e9
         peak, peak_kind = measured_peak()
