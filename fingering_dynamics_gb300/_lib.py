@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(PKG, "_lib", "libfdlbm.so")
 FD_OK = 0
 FD_F64, FD_F32, FD_F16, FD_BF16 = 0, 1, 2, 3
 FD_VARIANT_PERIODIC, FD_VARIANT_WALLS, FD_VARIANT_PERIODIC_XY = 0, 1, 2
-FD_INIT_MU, FD_INIT_UY, FD_INIT_VELOCITY = 1, 2, 4
+FD_INIT_MU, FD_INIT_UY, FD_INIT_VELOCITY, FD_OUTLET_PRESSURE = 1, 2, 4, 8
 FD_ROUND_NEAREST, FD_ROUND_STOCHASTIC = 0, 1
 ROUNDING = {"nearest": FD_ROUND_NEAREST, "stochastic": FD_ROUND_STOCHASTIC}
 TERMS = {"large_F": 0, "feq": 1, "geq": 2, "F": 3, "G": 4}

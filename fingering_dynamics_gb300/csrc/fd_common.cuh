@@ -53,6 +53,7 @@ struct Coef {
   T wsum_57;     // w5 + w7                        (fingering.py:362)
   T bx, by;      // body force per unit mass (FD_VARIANT_PERIODIC_XY; no reference counterpart)
   int body;      // 1: add the body force to the velocity and the forcing term
+  int p_out;     // 1: pressure outlet rho = 1 (FD_OUTLET_PRESSURE; no reference counterpart)
 };
 
 template <typename T>
@@ -81,6 +82,7 @@ inline Coef<T> make_coef(const fd_params& p) {
   c.body = p.variant == FD_VARIANT_PERIODIC_XY;
   c.bx = (T)(c.body ? p.force_x : 0.0);
   c.by = (T)(c.body ? p.force_y : 0.0);
+  c.p_out = (p.flags & FD_OUTLET_PRESSURE) ? 1 : 0;
   return c;
 }
 

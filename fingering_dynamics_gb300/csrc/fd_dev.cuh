@@ -45,6 +45,7 @@ struct DevCoef {
   float out_coef;      // 2/3 or 1.5
   float sf, inv_sf;    // storage scale of f deviations
   float sg, inv_sg;    // storage scale of g_1..g_8
+  int p_out;           // pressure outlet rho = 1 (FD_OUTLET_PRESSURE)
 };
 
 inline DevCoef make_dev_coef(const fd_params& p, int f_scale_log2, int g_scale_log2) {
@@ -67,6 +68,7 @@ inline DevCoef make_dev_coef(const fd_params& p, int f_scale_log2, int g_scale_l
   c.inv_sf = ldexpf(1.0f, -f_scale_log2);
   c.sg = ldexpf(1.0f, g_scale_log2);
   c.inv_sg = ldexpf(1.0f, -g_scale_log2);
+  c.p_out = (p.flags & FD_OUTLET_PRESSURE) ? 1 : 0;
   return c;
 }
 
@@ -262,8 +264,10 @@ __device__ __forceinline__ void dev_zou_he_f(const DevCoef& c, int variant, int 
   }
   if (x == W - 1) {                                        // fingering_periodic.py:312-324
     const float D = ((d[0] + d[2]) + d[4]) + 2.0f * ((d[1] + d[5]) + d[8]) + 0.5f * gx * mu;
-    const float a = ux * ((1.0f + D) * __frcp_rn(1.0f + ux));
-    d[3] = d[1] - c.out_coef * a + gm6;
+    // velocity outlet: a = u_x rho_out with rho_out = (1 + D) / (1 + u_x); pressure outlet
+    // (FD_OUTLET_PRESSURE): rho_out = 1 and u_x = D, so a = D and the coefficient is 2/3
+    const float a = c.p_out ? D : ux * ((1.0f + D) * __frcp_rn(1.0f + ux));
+    d[3] = d[1] - (c.p_out ? (2.0f / 3.0f) : c.out_coef) * a + gm6;
     d[6] = d[8] - 0.5f * (d[2] - d[4]) - (1.0f / 6.0f) * a + gm4 + gm6;
     d[7] = d[5] + 0.5f * (d[2] - d[4]) - (1.0f / 6.0f) * a - gm4 + gm6;
     if (variant == FD_VARIANT_WALLS) {                     // fingering.py:387-390

@@ -216,11 +216,23 @@ __device__ __forceinline__ void inlet_corner_top_g(const Coef<T>& c, T (&g)[9]) 
   g[7] = g[5];
 }
 
-// fingering_periodic.py:305-324 / fingering.py:369-385
+// fingering_periodic.py:305-324 / fingering.py:369-385.  With FD_OUTLET_PRESSURE
+// (an extension) rho_out = 1 is imposed instead and u_x = S / rho_out - 1
+// follows from the same known-population sum S; the coefficient of f3 is then
+// the standard 2/3, so that the outlet cell's density is exactly rho_out.
 template <typename T>
 __device__ __forceinline__ void outlet_f(const Coef<T>& c, T (&f)[9], T ux, T gx, T gy, T mu) {
-  const T r = (T(1) / (T(1) + ux)) * ((((f[0] + f[2]) + f[4]) + T(2) * ((f[1] + f[5]) + f[8])) + ((gx * mu) / T(2)));
-  f[3] = (f[1] - (c.out_coef * ux) * r) + ((gx * mu) / T(6));
+  const T S = (((f[0] + f[2]) + f[4]) + T(2) * ((f[1] + f[5]) + f[8])) + ((gx * mu) / T(2));
+  T r, coef;
+  if (c.p_out) {
+    r = T(1);
+    ux = S - T(1);
+    coef = c.two_thirds;
+  } else {
+    r = (T(1) / (T(1) + ux)) * S;
+    coef = c.out_coef;
+  }
+  f[3] = (f[1] - (coef * ux) * r) + ((gx * mu) / T(6));
   f[6] = (((f[8] - T(0.5) * (f[2] - f[4])) - (c.one_sixth * ux) * r) + ((gy * mu) / T(4))) + ((gx * mu) / T(6));
   f[7] = (((f[5] + T(0.5) * (f[2] - f[4])) - (c.one_sixth * ux) * r) - ((gy * mu) / T(4))) + ((gx * mu) / T(6));
 }

@@ -49,7 +49,8 @@ FIELD_NAMES = ("psi", "npx", "npy", "np2", "rho", "ux", "uy", "p", "mu", "mix_ta
 
 
 def make_fd_params(prm: LBMParams) -> L.fd_params:
-    flags = (L.FD_INIT_MU if prm.init_mu else 0) | (L.FD_INIT_UY if prm.init_uy else 0)
+    flags = ((L.FD_INIT_MU if prm.init_mu else 0) | (L.FD_INIT_UY if prm.init_uy else 0)
+             | (L.FD_OUTLET_PRESSURE if prm.outlet == "pressure" else 0))
     return L.fd_params(prm.H, prm.W, prm.variant_id, flags, prm.tau, prm.eta_n, prm.M, prm.a, prm.kappa,
                        prm.gamma, prm.psi_wall, prm.outlet_coef, prm.force_x, prm.force_y)
 

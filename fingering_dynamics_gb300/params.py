@@ -60,10 +60,13 @@ class LBMParams:
     inlet_ux: np.ndarray | None = field(default=None, repr=False)
     force_x: float = 0.0              # body force per unit mass, variant "periodic_xy" only
     force_y: float = 0.0
+    outlet: str = "velocity"          # "velocity" (the reference's) or "pressure" (rho = 1; an extension)
 
     def __post_init__(self):
         if self.variant not in _VARIANTS:
             raise ValueError(f"variant must be one of {sorted(_VARIANTS)}")
+        if self.outlet not in ("velocity", "pressure"):
+            raise ValueError("outlet must be 'velocity' or 'pressure'")
         if self.inlet_ux is None:
             self.inlet_ux = inlet_profile(self.H, self.u0, self.inlet)
         self.inlet_ux = np.ascontiguousarray(self.inlet_ux, dtype=np.float64)

@@ -55,6 +55,9 @@ enum fd_variant {
 /* fd_params.flags */
 #define FD_INIT_MU 1u /* Compute.__init__ evaluates mu before the equilibria (fingering.py:122) */
 #define FD_INIT_UY 2u /* ... and u_y with f = 0 (fingering.py:123) */
+#define FD_OUTLET_PRESSURE 8u /* extension, no reference counterpart: Zou-He pressure outlet rho = 1 at x = W-1
+                                 (u_x from the known populations, coefficient 2/3) instead of the reference's
+                                 velocity-type outlet; both variants, every kernel */
 #define FD_INIT_VELOCITY 4u /* fd_compute_init takes u_x, u_y from the fields' ux / uy arrays (the
                                equilibrium of a given flow: restarting from predicted fields; no
                                counterpart in the reference, whose runs start at rest) */

@@ -54,6 +54,9 @@ class OracleParams:
     # force per unit mass added to mu grad psi in the velocity and the forcing
     force_x: float = 0.0
     force_y: float = 0.0
+    # outlet "pressure" (also an extension): rho = 1 imposed at x = W-1, u_x from
+    # the known populations, coefficient 2/3, instead of the velocity-type outlet
+    outlet: str = "velocity"
 
 
 def gaussian_inlet_profile(H: int, u0: float) -> np.ndarray:
@@ -388,8 +391,13 @@ def zou_he_inlet_periodic(f, g, gx, gy, mu, prm):
 def _outlet_body(f, g, px, py, m, prm):
     ux = prm.inlet_ux
     c = prm.outlet_coef
-    rho_out = 1 / (1 + ux) * (f[0][:, -1] + f[2][:, -1] + f[4][:, -1]
-                              + 2 * (f[1][:, -1] + f[5][:, -1] + f[8][:, -1]) + px * m / 2)
+    S = (f[0][:, -1] + f[2][:, -1] + f[4][:, -1] + 2 * (f[1][:, -1] + f[5][:, -1] + f[8][:, -1]) + px * m / 2)
+    if prm.outlet == "pressure":
+        rho_out = np.ones_like(S)
+        ux = S - 1.0
+        c = 2 / 3
+    else:
+        rho_out = 1 / (1 + ux) * S
     psi_out = -1.0 - (g[0][:, -1] + g[1][:, -1] + g[2][:, -1] + g[4][:, -1] + g[5][:, -1] + g[8][:, -1])
     wsum = W9[3] + W9[6] + W9[7]
     f[3][:, -1] = f[1][:, -1] - c * ux * rho_out + px * m / 6

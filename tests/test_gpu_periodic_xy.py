@@ -87,3 +87,34 @@ def test_small_configuration_2000_steps_bitwise():
     assert np.array_equal(got["f"], st.f) and np.array_equal(got["g"], st.g)
     d = lat.diagnostics()
     assert np.isfinite(d["mass_r"]) and 0.0 < d["saturation"] < 1.0
+
+
+@pytest.mark.parametrize("variant", ["periodic", "walls"])
+def test_pressure_outlet_fp64_bitwise_and_packed_close(variant):
+    """The pressure-outlet extension (FD_OUTLET_PRESSURE) against the oracle's:
+    FP64 fused bit for bit, FP32 / FP16 storage within their tolerances."""
+    from dataclasses import replace
+    from fingering_dynamics_gb300 import geometry as geo
+    from fingering_dynamics_gb300.lattice import Lattice
+    from fingering_dynamics_gb300.params import from_relaxation_times
+    from oracle.lbm_oracle import OracleParams, OracleState
+    H, W = 32, 96
+    prm = replace(from_relaxation_times(H, W, 0.6, 1.0, 5e-4, 120.0, 0.01, variant=variant), outlet="pressure")
+    rects, circles = geo.random_blocks(H, W, 0.85, 3, 5, seed=7, x_margin=8)
+    g = geo.build_geometry(H, W, rects=rects, circles=circles, walls=variant == "walls")
+    op = OracleParams(H=H, W=W, variant=variant, tau=prm.tau, eta_n=prm.eta_n, M=prm.M, a=prm.a,
+                      kappa=prm.kappa, gamma=prm.gamma, psi_wall=prm.psi_wall, inlet_ux=prm.inlet_ux,
+                      outlet_coef=prm.outlet_coef, outlet="pressure")
+    walls = variant == "walls"
+    st = OracleState(op, g.solid, prm.initial_psi(g.solid), init_mu=walls, init_uy=walls)
+    for _ in range(60):
+        st.step(g.corner_list or None, g.circle_masks)
+    lat = Lattice(prm, g, dtype="f64")
+    lat.step(60)
+    got = lat.state()
+    assert np.array_equal(got["f"], st.f) and np.array_equal(got["g"], st.g)
+    m = ~g.solid
+    for dtype, tol in (("f32", 1e-5), ("f16", 1e-3)):
+        lp = Lattice(prm, g, dtype=dtype)
+        lp.step(60)
+        assert np.abs(lp.state()["psi"][m] - st.psi[m]).max() <= tol

@@ -53,3 +53,32 @@ def test_square_blocks_layout():
         assert x1 - x0 == 9 and y1 - y0 == 9 and x0 >= 2 and y0 >= 2 and x1 <= 253 and y1 <= 125
         occ[max(y0 - 1, 0):y1 + 2, max(x0 - 1, 0):x1 + 2] += 1   # gaps >= 2: 1-cell dilations never overlap
     assert occ.max() == 1
+
+
+def test_pressure_outlet_sets_unit_density():
+    """The pressure-outlet extension: after the outlet rule every outlet cell
+    holds exactly rho = 1 (the known-population sum fixes u_x; coefficient
+    2/3), in both variants (the walled variant's corner copies aside)."""
+    from fingering_dynamics_gb300 import geometry as geo
+    from fingering_dynamics_gb300.params import from_relaxation_times
+    for variant in ("periodic", "walls"):
+        H, W = 16, 48
+        prm = from_relaxation_times(H, W, 0.6, 1.0, 5e-4, 120.0, 0.01, variant=variant)
+        g = geo.build_geometry(H, W, walls=variant == "walls")
+        op = OracleParams(H=H, W=W, variant=variant, tau=prm.tau, eta_n=prm.eta_n, M=prm.M, a=prm.a,
+                          kappa=prm.kappa, gamma=prm.gamma, psi_wall=prm.psi_wall, inlet_ux=prm.inlet_ux,
+                          outlet_coef=prm.outlet_coef, outlet="pressure")
+        st = OracleState(op, g.solid, prm.initial_psi(g.solid), init_mu=variant == "walls",
+                         init_uy=variant == "walls")
+        rows = slice(1, -1) if variant == "walls" else slice(None)
+        for _ in range(30):
+            st.collide()
+            fb = st.f.copy()
+            gb = st.g.copy()
+            from oracle.lbm_oracle import bottom_top_wall, stream
+            st.f, st.g = stream(st.f), stream(st.g)
+            if variant == "walls":
+                bottom_top_wall(fb[:, 1:-1], gb[:, 1:-1], st.f[:, 1:-1], st.g[:, 1:-1])
+            st.zou_he()
+            assert np.allclose(np.sum(st.f[:, rows, -1], axis=0), 1.0, rtol=0, atol=1e-13)
+            st.macros()
