@@ -74,12 +74,11 @@ def ensemble_specs(n: int, seed: int, sizes_w=(256, 512, 1024, 2048), sizes_h=(1
     Family "spec" defaults to the ranges of the benchmark configuration
     (viscosity ratio 2..20, porosity 0.6..0.85, inlet 0.005..0.02).  Family
     "stable" defaults to viscosity ratio 2..5, porosity 0.70..0.85 and inlet
-    0.003..0.010: with the reference's velocity inlet and velocity outlet the
-    medium must carry the imposed flux with density differences of order
-    3 u nu L / k (Darcy), and denser or faster members crash (rho -> 0 at the
-    outlet) within a few thousand steps; on the 96-member draw of seed 2024
-    none of these diverges within 6000 steps, against 35 of 96 with the
-    configuration's porosity and inlet ranges."""
+    0.003..0.010: the medium must carry the imposed flux with density
+    differences of order 3 u nu L / k (Darcy), and denser or faster members
+    diverge within a few thousand steps (with either outlet rule); on the
+    96-member draw of seed 2024 none of these diverges within 6000 steps,
+    against 35 of 96 with the configuration's porosity and inlet ranges."""
     if ratio is None:
         ratio = (2.0, 20.0) if family == "spec" else (2.0, 5.0)
     if porosity is None:
