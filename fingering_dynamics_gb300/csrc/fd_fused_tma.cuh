@@ -24,6 +24,7 @@
 #pragma once
 
 #include "fd_fused_dev.cuh"
+#include "fd_host.h"
 
 namespace fd {
 
@@ -422,13 +423,9 @@ template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, char* pa,
                      char* pb, float* sa, float* sb, int nsteps, int R, uint32_t seed, cudaStream_t st) {
   using M = TmaSmem<SF, NT, NS>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(k_fused_tma<SF, NT, NS, SCALED, STOCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             M::BYTES) != cudaSuccess)
-      return FD_ERR_CUDA;
-    attr_set = true;
-  }
+  static std::atomic<unsigned long long> attr_done{0};
+  if (ensure_smem_attr(k_fused_tma<SF, NT, NS, SCALED, STOCH>, M::BYTES, attr_done) != cudaSuccess)
+    return FD_ERR_CUDA;
   const PackedLayout<SF> L = packed_layout<SF>(p.H, p.W);
   DevArgs<SF> a;
   a.c = c;

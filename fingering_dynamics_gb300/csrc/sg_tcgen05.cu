@@ -457,12 +457,9 @@ int launch_tch_r(const bf16* x, int N, int H, int W, int Cin, const bf16* w, con
                  bf16* z, bf16* y, cudaStream_t s) {
   using C = HaloCfg<BN, BK, R>;
   auto kern = k_conv3x3_tch<BN, BK, R>;
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) != cudaSuccess)
-      return fd::check_launch("sg_conv3x3_tc: shared-memory attribute");
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr_done{0};
+  if (fd::ensure_smem_attr(kern, C::SMEM, attr_done) != cudaSuccess)
+    return fd::check_launch("sg_conv3x3_tc: shared-memory attribute");
   dim3 grid((unsigned)((long long)N * (H / R) * (W / kTcBM)), (unsigned)(Cout / BN));
   kern<<<grid, kTcThreads, C::SMEM, s>>>(x, N, H, W, Cin, w, b, Cout, act, z, y);
   return fd::check_launch("sg_conv3x3_tc");
@@ -483,12 +480,9 @@ int launch_tc(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const 
               bf16* z, bf16* y, cudaStream_t s) {
   using C = TcCfg<BN, BK>;
   auto kern = k_conv3x3_tc<BN, BK>;
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) != cudaSuccess)
-      return fd::check_launch("sg_conv3x3_tc: shared-memory attribute");
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr_done{0};
+  if (fd::ensure_smem_attr(kern, C::SMEM, attr_done) != cudaSuccess)
+    return fd::check_launch("sg_conv3x3_tc: shared-memory attribute");
   const long long M = (long long)N * H * W;
   dim3 grid((unsigned)((M + kTcBM - 1) / kTcBM), (unsigned)(Cout / BN));
   kern<<<grid, kTcThreads, C::SMEM, s>>>(x, N, H, W, Cin, w, b, Cout, act, z, y);
