@@ -418,8 +418,8 @@ def run_surrogate(args):
     import torch
     from fingering_dynamics_gb300 import build
     from fingering_dynamics_gb300.ensemble import Ensemble, ensemble_specs
-    from fingering_dynamics_gb300.surrogate import (UNet, evaluate, expand, generate_trajectories,
-                                                    rollout_saturation_error, train)
+    from fingering_dynamics_gb300.surrogate import (UNet, accelerated_ensemble, evaluate, expand,
+                                                    generate_trajectories, rollout_saturation_error, train)
     build.build()
     H, W, jump = 256, 512, 200
     M = args.members
@@ -465,6 +465,9 @@ def run_surrogate(args):
     f1.record(stream)
     torch.cuda.synchronize()
     t_sur = f0.elapsed_time(f1) / 10 / 1e3
+    del frames, train_f, test_f, x
+    torch.cuda.empty_cache()
+    accel = accelerated_ensemble(net, [specs[i].build() for i in test_idx[:args.batch]], rounds=5, jump=jump)
     peak = None
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -486,6 +489,7 @@ def run_surrogate(args):
             "roofline": {"bound": "tensor", "achieved": round(tflops, 2), "peak": peak, "unit": "TFLOP/s",
                          "frac": round(tflops / peak, 4), "peak_kind": peak_kind, "traffic": None},
             "loss_history": hist, "held_out": ev, "rollout_saturation_rel_error": roll,
+            "accelerated_ensemble": accel,
             "jump_vs_lbm": {"members": nb, "lbm_200_iterations_ms": round(t_lbm * 1e3, 3),
                             "surrogate_jump_ms": round(t_sur * 1e3, 3), "speedup": round(t_lbm / t_sur, 2),
                             "speedup_with_judge": round(6 * t_lbm / (6 * t_sur + t_lbm), 2)},

@@ -107,9 +107,22 @@ class Ensemble:
         ``rounding``: FP16/BF16 store rounding (stochastic by default); member
         k's stochastic-rounding seed is k, its steps use seed + iteration as
         they would when advanced alone."""
-        self.lattices = [Lattice(m[0], m[1], dtype=dtype, device=device, psi0=m[2] if len(m) > 2 else None,
-                                 rounding=rounding, seed=k)
-                         for k, m in enumerate(members)]
+        lattices = [Lattice(m[0], m[1], dtype=dtype, device=device, psi0=m[2] if len(m) > 2 else None,
+                            rounding=rounding, seed=k)
+                    for k, m in enumerate(members)]
+        self._attach(lattices, rows_per_strip, band_width)
+
+    @classmethod
+    def from_lattices(cls, lattices, rows_per_strip: int = 32, band_width: int = 128) -> "Ensemble":
+        """A batch over existing lattices (same packed storage type), in their
+        current state: lattices in reference mode enter the fused state here."""
+        ens = cls.__new__(cls)
+        ens._batch = C.c_void_p()
+        ens._attach(list(lattices), rows_per_strip, band_width)
+        return ens
+
+    def _attach(self, lattices, rows_per_strip, band_width):
+        self.lattices = lattices
         for lat in self.lattices:
             if lat.storage is None:
                 raise ValueError("ensembles use packed storage: dtype f32, f16 or bf16")

@@ -248,6 +248,24 @@ class Lattice:
         if iteration is not None:
             self.iteration = int(iteration)
 
+    def checkpoint(self) -> dict:
+        """In-memory copy of a reference-mode state (populations, boundary
+        values, fields, iteration) for :meth:`restore`."""
+        self._require("reference")
+        ck = {"pop": self.pop[self.cur].clone(), "side": self.side[self.scur].clone(), "iteration": self.iteration}
+        for n in FIELD_NAMES:
+            ck[n] = getattr(self, n).clone()
+        return ck
+
+    def restore(self, ck: dict):
+        """Return to a state taken by :meth:`checkpoint` (reference mode)."""
+        self.mode = "reference"
+        self.pop[self.cur].copy_(ck["pop"])
+        self.side[self.scur].copy_(ck["side"])
+        for n in FIELD_NAMES:
+            getattr(self, n).copy_(ck[n])
+        self.iteration = ck["iteration"]
+
     def step_seed(self) -> int:
         """Stochastic-rounding seed of the next fused launch."""
         return (self.seed + self.iteration) & 0xFFFFFFFF

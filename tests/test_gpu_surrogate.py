@@ -208,3 +208,18 @@ def test_tcgen05_conv_matches_oracle(n, h, w, cin, cout, act):
     assert np.abs(ytc - yr).max() <= 1e-2 * scale
     # the two tensor-core paths round their FP32 sums to the same bfloat16 almost everywhere
     assert np.mean(ztc != outs["sg_conv3x3"][0]) < 0.02
+
+
+def test_accelerated_ensemble_runs_to_the_horizon():
+    """The accelerated ensemble (batched jumps, batched LBM judge, exact
+    restore and plain fallback) reaches the same iteration as the plain
+    batched run, with finite states; an untrained network (persistence) is
+    mostly rejected by the judge."""
+    from fingering_dynamics_gb300.ensemble import ensemble_specs
+    from fingering_dynamics_gb300.surrogate import UNet, accelerated_ensemble
+    members = [s.build() for s in ensemble_specs(4, seed=21, sizes_w=(128,), sizes_h=(64,))]
+    net = UNet((16, 32, 32, 64), seed=0)
+    r = accelerated_ensemble(net, members, rounds=2, jumps_per_check=2, jump=50)
+    assert r["horizon_iterations"] == 2 * 3 * 50
+    assert r["member_rounds"] == 8 and 0 <= r["accepted_rounds"] <= 8
+    assert np.isfinite(r["final_saturation_rel_error_mean"]) and r["plain_s"] > 0 and r["accelerated_s"] > 0
