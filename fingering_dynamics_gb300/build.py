@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import argparse
 import concurrent.futures as cf
+import fcntl
 import hashlib
 import os
 import shutil
@@ -60,15 +61,34 @@ def _sources_digest(extra: list[str]) -> str:
     return h.hexdigest()
 
 
+def _up_to_date(stamp: str, digest: str) -> bool:
+    if not (os.path.exists(LIB) and os.path.exists(stamp)):
+        return False
+    with open(stamp) as fh:
+        return fh.read().strip() == digest
+
+
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
+    """Compile and link when the sources changed.  Concurrent callers (one per
+    rank of a multi-GPU run) serialise on a lock file; the later ones find the
+    library already built."""
     os.makedirs(OUT, exist_ok=True)
     extra = ["-Xptxas", "-v"] if ptxas_info else []
     digest = _sources_digest(extra)
     stamp = os.path.join(OUT, "libfdlbm.sha256")
-    if not force and os.path.exists(LIB) and os.path.exists(stamp):
-        with open(stamp) as fh:
-            if fh.read().strip() == digest:
+    if not force and _up_to_date(stamp, digest):
+        return LIB
+    with open(os.path.join(OUT, ".build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            if not force and _up_to_date(stamp, digest):
                 return LIB
+            return _compile_and_link(digest, stamp, extra, verbose)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _compile_and_link(digest: str, stamp: str, extra: list, verbose: bool) -> str:
     cc = nvcc()
     objs = []
 

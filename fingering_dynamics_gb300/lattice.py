@@ -242,9 +242,10 @@ class Lattice:
         rho_d = None if rho is None else torch.as_tensor(rho, device=dev).to(torch.float64).contiguous()
         prm = L.fd_params.from_buffer_copy(self.prm)
         prm.flags |= L.FD_INIT_MU | L.FD_INIT_VELOCITY
+        # psi_d / rho_d were allocated on this stream, so the caching allocator
+        # reuses their memory only for work ordered after the init kernels
         L.call("fd_compute_init", C.byref(prm), self.fd_dtype, _ptr(self.mask), _ptr(psi_d), _ptr(rho_d),
                C.byref(self.fields()), self._stream())
-        torch.cuda.current_stream(self.device).synchronize()
         if iteration is not None:
             self.iteration = int(iteration)
 
