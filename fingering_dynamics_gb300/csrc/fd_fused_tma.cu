@@ -44,7 +44,24 @@ int fused_tma(const fd_params& p, const fd_storage& st, const DevCoef& c, const 
 
 int tma_band_width() { return FD_TMA_NT; }
 
+// One thread waits, through the staged kernel's bounded wait, on an mbarrier
+// that nothing arrives on: the wait gives up after `polls` polls and latches
+// bit 0 of the device error word (the failure path of the kernel, exercised
+// without a fault or a hang).
+__global__ void k_selftest_wait_timeout(unsigned polls) {
+  __shared__ uint64_t bar;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  mbar_wait(&bar, 0u, polls);
+}
+
 }  // namespace fd
+
+extern "C" int fd_selftest_wait_timeout(unsigned polls, void* stream) {
+  FD_REQUIRE(polls >= 1 && polls <= (1u << 20), FD_ERR_ARG, "fd_selftest_wait_timeout: polls in [1, 2^20]");
+  fd::k_selftest_wait_timeout<<<1, 1, 0, fd::as_stream(stream)>>>(polls);
+  return fd::check_launch("fd_selftest_wait_timeout");
+}
 
 extern "C" int fd_device_status(unsigned* out, int clear) {
   FD_REQUIRE(out != nullptr, FD_ERR_ARG, "fd_device_status: NULL pointer");

@@ -52,11 +52,11 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       : "memory");
 }
 
-// Wait for phase `parity` of an mbarrier, at most kWaitLimit polls.  Returns
+// Wait for phase `parity` of an mbarrier, at most `limit` polls.  Returns
 // false (and latches the device error word) if the phase never completed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned limit = kWaitLimit) {
   const uint32_t a = smem_u32(bar);
-  for (unsigned it = 0; it < kWaitLimit; ++it) {
+  for (unsigned it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

@@ -333,6 +333,13 @@ size_t fd_diag_scratch_bytes(void);
 int fd_diagnostics(const fd_params* prm, int dtype, const fd_storage* st, const void* pop, const uint16_t* mask,
                    void* scratch, fd_diag* out, void* stream);
 
+/* Self-test of the failure path: one thread waits, through the staged kernel's
+ * bounded mbarrier wait, on a barrier that nothing arrives on; after `polls`
+ * polls (1 .. 2^20) the wait gives up and bit 0 of the device error word is set
+ * (read with fd_device_status).  Faults, traps and hangs nothing.  No
+ * counterpart in the reference. */
+int fd_selftest_wait_timeout(unsigned polls, void* stream);
+
 /* Device-side status word of the library's kernels (bit 0: a bounded wait on
  * an asynchronous copy gave up).  Copies it to *out and, if clear != 0,
  * resets it.  Synchronous.  No counterpart in the reference (numpy raises

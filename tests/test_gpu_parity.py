@@ -178,6 +178,25 @@ def test_device_status_clean_after_runs():
     assert v.value == 0
 
 
+def test_bounded_wait_gives_up_and_the_context_stays_usable():
+    """A wait on an mbarrier that nothing arrives on gives up after a short
+    poll limit, latches the status bit, and the next step runs normally."""
+    import ctypes as C
+    from fingering_dynamics_gb300 import _lib as L
+    v = C.c_uint(0)
+    L.call("fd_device_status", C.byref(v), 1)
+    L.call("fd_selftest_wait_timeout", 1000, None)
+    torch.cuda.synchronize()
+    L.call("fd_device_status", C.byref(v), 1)
+    assert v.value & 1
+    fx = load("walls_rects_24x48")
+    lat = make_lattice(fx, "f32")
+    lat.step(5)
+    torch.cuda.synchronize()
+    L.call("fd_device_status", C.byref(v), 0)
+    assert v.value == 0 and bool(torch.isfinite(lat.psi).all())
+
+
 @pytest.mark.parametrize("name", LONG)
 def test_fused_500_steps_fp32_exact_order(name):
     """FP32 with the reference's operand order: a looser 5e-5 bound (its
