@@ -183,7 +183,7 @@ __device__ __forceinline__ float psi_cell(const char* sm, const DevArgs<SF>& a, 
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int strip, char* smem, unsigned& phase,
                                           bool& ok) {
-  static_assert(NS == 5, "the slot rotation below keeps rows y-2 .. y+2 in five slots");
+  static_assert(NS >= 5, "rows y-2 .. y+2 must be resident while row y is computed");
   using L = SlotLayout<SF, NT>;
   using M = TmaSmem<SF, NT, NS>;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
@@ -201,7 +201,7 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
   const int hl = (t == NT / 2) ? -1 : (t == NT - 1 ? NT : 0);
   const bool halo = (t == NT / 2) || (t == NT - 1);
 
-  // row first + k lives in slot k (mod 5); rows y0-2 .. y0+2 fill slots 0..4
+  // row first + k lives in slot k (mod NS); rows y0-2 .. y0+NS-3 fill slots 0..NS-1
   if (t == 0) {
     for (int k = 0; k < NS && first + k <= last; ++k)
       issue_row<SF, NT>(a, smem + M::OFF_SLOT + k * L::BYTES, &bars[k], first + k, x0);
@@ -210,11 +210,11 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
     if (ok) ok = mbar_wait(&bars[s], (phase >> s) & 1u);
     phase ^= 1u << s;
   };
-  // slots of rows y-2, y-1, y, y+1, y+2 (rotated every row) and their byte offsets
-  int si[5], so[5];
+  // slots of rows y-2 .. y+NS-3 (rotated every row) and their byte offsets
+  int si[NS], so[NS];
 #pragma unroll
-  for (int k = 0; k < 5; ++k) {
-    si[k] = k;  // rows y0-2 .. y0+2
+  for (int k = 0; k < NS; ++k) {
+    si[k] = k;  // rows y0-2 .. y0+NS-3
     so[k] = M::OFF_SLOT + k * L::BYTES;
   }
   int pslot = 0;  // psi ring slot of row y0-1; rows y0-1, y0, y0+1 use pslot, +1, +2 (mod 4)
@@ -273,9 +273,9 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
       pull_cell<SF, NT, false, SCALED>(smem, a.c, prow, t, mask_at<SF, NT>(smem, prow[1], t) & 0xFFu, fn);
       drho_nb = dev_inlet_drho(fn, (float)a.inlet_ux[yn], a.side_in[0 * a.H + yn], a.side_in[2 * a.H + yn]);
     }
-    // 2. psi(y+1) complete; the slot of row y-2 is free for row y+3
+    // 2. psi(y+1) complete; the slot of row y-2 is free for row y+NS-2
     __syncthreads();
-    if (t == 0 && y + 3 <= last) issue_row<SF, NT>(a, smem + so[0], &bars[si[0]], y + 3, x0);
+    if (t == 0 && y + NS - 2 <= last) issue_row<SF, NT>(a, smem + so[0], &bars[si[0]], y + NS - 2, x0);
     // 3. stencils, f pull, Zou-He, collision, store
     if (owned) {
       const float* pm = psi_row(0);
@@ -331,15 +331,15 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
     for (int i = 0; i < 9; ++i) gC[i] = gN[i];
     pS = pC;
     pC = pN;
-    // rotate: rows y-1 .. y+3 become y-2 .. y+2 for the next row
+    // rotate: rows y-1 .. y+NS-2 become y-2 .. y+NS-3 for the next row
     const int freed = si[0], freed_off = so[0];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < NS - 1; ++k) {
       si[k] = si[k + 1];
       so[k] = so[k + 1];
     }
-    si[4] = freed;
-    so[4] = freed_off;
+    si[NS - 1] = freed;
+    so[NS - 1] = freed_off;
     pslot = (pslot + 1) & 3;
   }
   // After a wait gave up, make sure the last copy issued into every slot has
