@@ -27,8 +27,6 @@ struct fd_batch {
 namespace fd {
 namespace {
 
-constexpr int kNS = 5;
-
 template <typename SF>
 DevArgs<SF> instance_args(const fd_instance& in, const fd_storage& st, int rows, bool swap) {
   const fd_params& p = in.prm;
@@ -61,8 +59,8 @@ DevArgs<SF> instance_args(const fd_instance& in, const fd_storage& st, int rows,
 
 template <typename SF, int NT, bool STOCH>
 int prepare(fd_batch* b) {
-  using M = TmaSmem<SF, NT, kNS>;
-  auto kern = k_fused_tma_batch<SF, NT, kNS, false, STOCH>;
+  using M = TmaSmem<SF, NT, tma_ring_depth<SF>()>;
+  auto kern = k_fused_tma_batch<SF, NT, tma_ring_depth<SF>(), false, STOCH>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, M::BYTES) != cudaSuccess)
     return check_launch("fd_batch: shared-memory attribute");
   std::vector<BatchInst<SF>> hi(b->n);
@@ -97,8 +95,8 @@ int prepare(fd_batch* b) {
 
 template <typename SF, int NT, bool STOCH>
 void launch_one(const fd_batch* b, int parity, cudaStream_t st) {
-  using M = TmaSmem<SF, NT, kNS>;
-  k_fused_tma_batch<SF, NT, kNS, false, STOCH><<<b->grid, NT, M::BYTES, st>>>(
+  using M = TmaSmem<SF, NT, tma_ring_depth<SF>()>;
+  k_fused_tma_batch<SF, NT, tma_ring_depth<SF>(), false, STOCH><<<b->grid, NT, M::BYTES, st>>>(
       (const BatchInst<SF>*)b->d_inst, b->d_tiles, b->ntiles, parity, b->d_steps);
 }
 

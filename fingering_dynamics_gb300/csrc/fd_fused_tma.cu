@@ -3,13 +3,6 @@
 #include "fd_fused_tma.cuh"
 #include "fd_host.h"
 
-#ifndef FD_TMA_NT
-#define FD_TMA_NT 128
-#endif
-#ifndef FD_TMA_NS
-#define FD_TMA_NS 5
-#endif
-
 namespace fd {
 
 template <typename SF, bool STOCH>
@@ -17,9 +10,9 @@ int fused_tma_r(const fd_params& p, const fd_storage& st, const DevCoef& c, cons
                 const double* inlet_ux, void* pa, void* pb, void* sa, void* sb, int nsteps, int R, cudaStream_t s) {
   const bool scaled = st.f_scale_log2 != 0 || st.g_scale_log2 != 0;
   if (scaled)
-    return launch_fused_tma<SF, FD_TMA_NT, FD_TMA_NS, true, STOCH>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
+    return launch_fused_tma<SF, FD_TMA_NT, tma_ring_depth<SF>(), true, STOCH>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
                                                                    (float*)sa, (float*)sb, nsteps, R, st.seed, s);
-  return launch_fused_tma<SF, FD_TMA_NT, FD_TMA_NS, false, STOCH>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
+  return launch_fused_tma<SF, FD_TMA_NT, tma_ring_depth<SF>(), false, STOCH>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
                                                                   (float*)sa, (float*)sb, nsteps, R, st.seed, s);
 }
 
@@ -37,7 +30,7 @@ int fused_tma(const fd_params& p, const fd_storage& st, const DevCoef& c, const 
     case FD_F16: return fused_tma_t<__half>(p, st, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, s);
     case FD_BF16: return fused_tma_t<__nv_bfloat16>(p, st, c, mask, inlet_ux, pa, pb, sa, sb, nsteps, R, s);
     default:
-      return launch_fused_tma<float, FD_TMA_NT, FD_TMA_NS, false, false>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
+      return launch_fused_tma<float, FD_TMA_NT, tma_ring_depth<float>(), false, false>(p, c, mask, inlet_ux, (char*)pa, (char*)pb,
                                                                          (float*)sa, (float*)sb, nsteps, R, 0, s);
   }
 }

@@ -3,11 +3,16 @@
 //
 // A CTA of NT threads owns a band of NT consecutive cells of every row of a
 // strip of R rows and marches down the strip.  Shared memory holds a ring of
-// NS row slots; a slot holds one lattice row of all 18 population planes and
-// of the mask word, for the band plus a 16-byte halo on each side.  One
-// thread issues the bulk copies of row y + NS - 2 while the CTA works on row
-// y, so global-memory latency is covered by the rows in flight instead of by
-// warps waiting on loads.
+// row slots; a slot holds one lattice row of all 18 population planes for the
+// band plus a 16-byte halo on each side.  One thread issues the bulk copies of
+// rows ahead while the CTA works on row y, so global-memory latency is covered
+// by the rows in flight instead of by warps waiting on loads.  Two rings:
+//   NS >= 5 whole-row slots (with the mask row), one mbarrier each; row
+//     y + NS - 2 is issued at row y (FP16 / BF16 storage);
+//   NS == 4 split slots whose f half and g half complete on separate
+//     mbarriers and are refilled as soon as each is no longer read, with the
+//     mask rows in a ring of their own (FP32 storage: the smaller footprint
+//     fits 5 CTAs per SM instead of 4).
 //
 // Per row y, each thread (one cell x = x0 + t):
 //   1. pulls g of row y+1 from the ring (stream + bounce-back + Zou-He g,
@@ -26,7 +31,27 @@
 #include "fd_fused_dev.cuh"
 #include "fd_host.h"
 
+// Band width (threads per CTA) of the single-lattice launch, and ring depth
+// per storage type for both launches (NS == 4: the split ring; NS >= 5:
+// whole-row slots).  Measured on 4096 x 2048: FP32 (memory-bound) gains 9% on
+// the split ring, which fits 5 CTAs per SM instead of 4; FP16/BF16
+// (issue-bound) lose 5% on it and keep five whole-row slots.
+#ifndef FD_TMA_NT
+#define FD_TMA_NT 128
+#endif
+#ifndef FD_TMA_NS_F32
+#define FD_TMA_NS_F32 4
+#endif
+#ifndef FD_TMA_NS_16
+#define FD_TMA_NS_16 5
+#endif
+
 namespace fd {
+
+template <typename SF>
+constexpr int tma_ring_depth() {
+  return std::is_same_v<SF, float> ? FD_TMA_NS_F32 : FD_TMA_NS_16;
+}
 
 // Device-side error word: bit 0 = an mbarrier wait gave up (copy never
 // completed).  Read and cleared by fd_device_status().  This header is
@@ -84,38 +109,94 @@ struct SlotLayout {
   static constexpr int BYTES = (OFF_M + RM + 127) / 128 * 128;
 };
 
+// Shared memory of the staged kernel.  NS >= 5: a ring of NS whole-row slots
+// (f, g and mask of a row behind one mbarrier).  NS == 4: the split ring, four
+// slots whose f half and g half complete on separate mbarriers (0..3: g half
+// and mask row, 4..7: f half), without the mask; the mask rows live in a ring
+// of their own (8 rows) and arrive with the g half.
 template <typename SF, int NT, int NS>
 struct TmaSmem {
+  using L = SlotLayout<SF, NT>;
+  static constexpr bool SPLIT = NS == 4;
+  static constexpr int NBAR = SPLIT ? 8 : NS;
   static constexpr int PSI_ROW = NT + 2;
   static constexpr int OFF_BAR = 0;
   static constexpr int OFF_PSI = 128;
-  static constexpr int OFF_SLOT = (OFF_PSI + 4 * PSI_ROW * 4 + 127) / 128 * 128;
-  static constexpr int BYTES = OFF_SLOT + NS * SlotLayout<SF, NT>::BYTES;
+  static constexpr int OFF_MASK = (OFF_PSI + 4 * PSI_ROW * 4 + 127) / 128 * 128;
+  static constexpr int MASK_ROWS = SPLIT ? 8 : 0;
+  static constexpr int OFF_SLOT = (OFF_MASK + MASK_ROWS * L::RM + 127) / 128 * 128;
+  static constexpr int SLOT = SPLIT ? (L::OFF_M + 127) / 128 * 128 : L::BYTES;
+  static constexpr int BYTES = OFF_SLOT + NS * SLOT;
+  static_assert(NBAR * 8 <= OFF_PSI, "mbarriers overlap the psi ring");
 };
 
-// Issue the bulk copies of lattice row r (wrapped into [0, H)) into slot s.
+// The part of lattice row r (wrapped into [0, H)) that a band loads: per kind
+// of plane the first loaded cell, the bytes per plane row and the byte offset
+// of the first loaded cell within the slot row (the band's halo is clipped at
+// the lattice's x edges).
+template <typename SF, int NT>
+struct RowSpan {
+  size_t rowoff;
+  int xs, gs, ms;
+  unsigned nf, ng, nm;
+  int df, dg, dm;
+  __device__ __forceinline__ RowSpan(int r, int x0, int H, int W) {
+    using L = SlotLayout<SF, NT>;
+    rowoff = (size_t)wrap(r, H) * W;
+    xs = max(x0 - L::HF, 0);
+    gs = max(x0 - L::HG, 0);
+    ms = max(x0 - L::HM, 0);
+    nf = (unsigned)((min(x0 + NT + L::HF, W) - xs) * (int)sizeof(SF));
+    ng = (unsigned)((min(x0 + NT + L::HG, W) - gs) * 4);
+    nm = (unsigned)((min(x0 + NT + L::HM, W) - ms) * 2);
+    df = (xs - (x0 - L::HF)) * (int)sizeof(SF);
+    dg = (gs - (x0 - L::HG)) * 4;
+    dm = (ms - (x0 - L::HM)) * 2;
+  }
+};
+
+template <typename SF, int NT>
+__device__ __forceinline__ void copy_f_half(const DevArgs<SF>& a, char* slot, uint64_t* bar, const RowSpan<SF, NT>& s) {
+  using L = SlotLayout<SF, NT>;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) bulk_g2s(slot + i * L::RF + s.df, a.src_f + i * a.pstride_f + s.rowoff + s.xs, s.nf, bar);
+}
+
+template <typename SF, int NT>
+__device__ __forceinline__ void copy_g_half(const DevArgs<SF>& a, char* slot, uint64_t* bar, const RowSpan<SF, NT>& s) {
+  using L = SlotLayout<SF, NT>;
+  bulk_g2s(slot + L::OFF_G0 + s.dg, a.src_g0 + s.rowoff + s.gs, s.ng, bar);
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    bulk_g2s(slot + L::OFF_GI + i * L::RF + s.df, a.src_gi + i * a.pstride_f + s.rowoff + s.xs, s.nf, bar);
+}
+
+// Issue the bulk copies of lattice row r into a whole-row slot (NS >= 5).
 template <typename SF, int NT>
 __device__ __forceinline__ void issue_row(const DevArgs<SF>& a, char* slot, uint64_t* bar, int r, int x0) {
   using L = SlotLayout<SF, NT>;
-  const int y = wrap(r, a.H);
-  const size_t rowoff = (size_t)y * a.W;
-  auto span = [&](int halo, int& xs, int& xe) {
-    xs = max(x0 - halo, 0);
-    xe = min(x0 + NT + halo, a.W);
-  };
-  int xs, xe, gs, ge, ms, me;
-  span(L::HF, xs, xe);
-  span(L::HG, gs, ge);
-  span(L::HM, ms, me);
-  const unsigned nf = (unsigned)((xe - xs) * sizeof(SF)), ng = (unsigned)((ge - gs) * 4), nm = (unsigned)((me - ms) * 2);
-  mbar_expect_tx(bar, 17 * nf + ng + nm);
-  const int df = (xs - (x0 - L::HF)) * (int)sizeof(SF), dg = (gs - (x0 - L::HG)) * 4, dm = (ms - (x0 - L::HM)) * 2;
-#pragma unroll
-  for (int i = 0; i < 9; ++i) bulk_g2s(slot + i * L::RF + df, a.src_f + i * a.pstride_f + rowoff + xs, nf, bar);
-  bulk_g2s(slot + L::OFF_G0 + dg, a.src_g0 + rowoff + gs, ng, bar);
-#pragma unroll
-  for (int i = 0; i < 8; ++i) bulk_g2s(slot + L::OFF_GI + i * L::RF + df, a.src_gi + i * a.pstride_f + rowoff + xs, nf, bar);
-  bulk_g2s(slot + L::OFF_M + dm, a.mask + rowoff + ms, nm, bar);
+  const RowSpan<SF, NT> s(r, x0, a.H, a.W);
+  mbar_expect_tx(bar, 17 * s.nf + s.ng + s.nm);
+  copy_f_half<SF, NT>(a, slot, bar, s);
+  copy_g_half<SF, NT>(a, slot, bar, s);
+  bulk_g2s(slot + L::OFF_M + s.dm, a.mask + s.rowoff + s.ms, s.nm, bar);
+}
+
+// Split ring (NS == 4): the g half of row r with its mask row, and the f half.
+template <typename SF, int NT>
+__device__ __forceinline__ void issue_g_half(const DevArgs<SF>& a, char* slot, char* mrow, uint64_t* bar, int r,
+                                             int x0) {
+  const RowSpan<SF, NT> s(r, x0, a.H, a.W);
+  mbar_expect_tx(bar, 8 * s.nf + s.ng + s.nm);
+  copy_g_half<SF, NT>(a, slot, bar, s);
+  bulk_g2s(mrow + s.dm, a.mask + s.rowoff + s.ms, s.nm, bar);
+}
+
+template <typename SF, int NT>
+__device__ __forceinline__ void issue_f_half(const DevArgs<SF>& a, char* slot, uint64_t* bar, int r, int x0) {
+  const RowSpan<SF, NT> s(r, x0, a.H, a.W);
+  mbar_expect_tx(bar, 9 * s.nf);
+  copy_f_half<SF, NT>(a, slot, bar, s);
 }
 
 // Shared-memory load of element idx of a plane row at byte offset `off` from
@@ -156,20 +237,22 @@ __device__ __forceinline__ void pull_cell(const char* sm, const DevCoef& c, cons
   }
 }
 
+// Mask word of band cell lx; `mrow` is the byte offset of the mask row.
 template <typename SF, int NT>
-__device__ __forceinline__ unsigned mask_at(const char* sm, int row, int lx) {
+__device__ __forceinline__ unsigned mask_at(const char* sm, int mrow, int lx) {
   using L = SlotLayout<SF, NT>;
-  return reinterpret_cast<const uint16_t*>(sm + row + L::OFF_M)[lx + L::HM];
+  return reinterpret_cast<const uint16_t*>(sm + mrow)[lx + L::HM];
 }
 
 // psi of cell x (band index lx) of row y from its pulled g after Zou-He
 // (fingering_periodic.py:210-212, 278-302); the pulled g is returned in g.
+// `mrow` is the byte offset of row y's mask row.
 template <typename SF, int NT, bool SCALED>
-__device__ __forceinline__ float psi_cell(const char* sm, const DevArgs<SF>& a, const int (&rows)[3], int x, int lx,
-                                          int y, float (&g)[9]) {
+__device__ __forceinline__ float psi_cell(const char* sm, const DevArgs<SF>& a, const int (&rows)[3], int mrow, int x,
+                                          int lx, int y, float (&g)[9]) {
   if (x < 0) return 1.0f;
   if (x >= a.W) return -1.0f;
-  const unsigned m = mask_at<SF, NT>(sm, rows[1], lx);
+  const unsigned m = mask_at<SF, NT>(sm, mrow, lx);
   pull_cell<SF, NT, true, SCALED>(sm, a.c, rows, lx, m & 0xFFu, g);
   if (x == 0 || x == a.W - 1) dev_zou_he_g(a.c, a.variant, a.H, a.W, x, y, g);
   if (m & SOLID) return a.c.psi_wall;
@@ -181,8 +264,8 @@ __device__ __forceinline__ float psi_cell(const char* sm, const DevArgs<SF>& a, 
 // (per-slot parity of the next fill to wait for) and `ok` carry over from
 // strip to strip.  Ends with a CTA barrier, so the ring can be refilled.
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
-__device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int strip, char* smem, unsigned& phase,
-                                          bool& ok) {
+__device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, int band, int strip, char* smem, unsigned& phase,
+                                               bool& ok) {
   static_assert(NS >= 5, "rows y-2 .. y+2 must be resident while row y is computed");
   using L = SlotLayout<SF, NT>;
   using M = TmaSmem<SF, NT, NS>;
@@ -204,7 +287,7 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
   // row first + k lives in slot k (mod NS); rows y0-2 .. y0+NS-3 fill slots 0..NS-1
   if (t == 0) {
     for (int k = 0; k < NS && first + k <= last; ++k)
-      issue_row<SF, NT>(a, smem + M::OFF_SLOT + k * L::BYTES, &bars[k], first + k, x0);
+      issue_row<SF, NT>(a, smem + M::OFF_SLOT + k * M::SLOT, &bars[k], first + k, x0);
   }
   auto wait_slot = [&](int s) {
     if (ok) ok = mbar_wait(&bars[s], (phase >> s) & 1u);
@@ -215,7 +298,7 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
 #pragma unroll
   for (int k = 0; k < NS; ++k) {
     si[k] = k;  // rows y0-2 .. y0+NS-3
-    so[k] = M::OFF_SLOT + k * L::BYTES;
+    so[k] = M::OFF_SLOT + k * M::SLOT;
   }
   int pslot = 0;  // psi ring slot of row y0-1; rows y0-1, y0, y0+1 use pslot, +1, +2 (mod 4)
   auto psi_row = [&](int k) { return psi_ring + ((pslot + k) & 3) * M::PSI_ROW; };
@@ -234,13 +317,13 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
     float* pr = psi_row(k);
     const bool ghost = walls && (r < 0 || r >= a.H);
     const int yr = wrap(r, a.H);
-    const float pv = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x, t, yr, gN);
+    const float pv = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x, t, yr, gN);
     pr[t + 1] = pv;
     if (k == 0) pS = pv;
     else pC = pv;
     if (halo) {
       float gh[9];
-      pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x0 + hl, hl, yr, gh);
+      pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x0 + hl, hl, yr, gh);
     }
   }
 #pragma unroll
@@ -255,11 +338,11 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
       const bool ghost = walls && (y + 1 >= a.H);
       const int yr = wrap(y + 1, a.H);
       float* pr = psi_row(2);
-      pN = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x, t, yr, gN);
+      pN = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x, t, yr, gN);
       pr[t + 1] = pN;
       if (halo) {
         float gh[9];
-        pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, x0 + hl, hl, yr, gh);
+        pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x0 + hl, hl, yr, gh);
       }
     }
     // rho_inlet - 1 of row 1 (bottom inlet corner, rows 0..2 = y..y+2) or of
@@ -270,7 +353,7 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
       const int prow[3] = {y == 0 ? so[2] : so[0], y == 0 ? so[3] : so[1], y == 0 ? so[4] : so[2]};
       const int yn = (y == 0) ? 1 : a.H - 2;
       float fn[9];
-      pull_cell<SF, NT, false, SCALED>(smem, a.c, prow, t, mask_at<SF, NT>(smem, prow[1], t) & 0xFFu, fn);
+      pull_cell<SF, NT, false, SCALED>(smem, a.c, prow, t, mask_at<SF, NT>(smem, prow[1] + L::OFF_M, t) & 0xFFu, fn);
       drho_nb = dev_inlet_drho(fn, (float)a.inlet_ux[yn], a.side_in[0 * a.H + yn], a.side_in[2 * a.H + yn]);
     }
     // 2. psi(y+1) complete; the slot of row y-2 is free for row y+NS-2
@@ -288,7 +371,7 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
       const float gy = (4.0f * (N - S) + ((NE + NW) - (SE + SW))) * (1.0f / 12.0f);
       const float lap = (4.0f * ((N + S) + (E + Wv)) + ((NE + NW) + (SE + SW)) - 20.0f * C) * (1.0f / 6.0f);
       const int rows[3] = {so[1], so[2], so[3]};
-      const unsigned m = mask_at<SF, NT>(smem, rows[1], t);
+      const unsigned m = mask_at<SF, NT>(smem, rows[1] + L::OFF_M, t);
       float f[9];
       pull_cell<SF, NT, false, SCALED>(smem, a.c, rows, t, m & 0xFFu, f);
       if (x == 0 || x == a.W - 1) {
@@ -355,12 +438,212 @@ __device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int st
   ok = __syncthreads_and(ok);
 }
 
+// rho_inlet - 1 of row yn (1 or H-2) of the walled variant's inlet column
+// (fingering.py:341, 357) from f pulled straight from global memory.  Only the
+// directions dev_inlet_drho reads (e_x <= 0) are loaded; the others stay 0.
+template <typename SF, bool SCALED>
+__device__ __forceinline__ float inlet_corner_drho(const DevArgs<SF>& a, int yn) {
+  const unsigned bits = a.mask[(size_t)yn * a.W] & 0xFFu;
+  auto ld = [&](int i, int y, int x) -> float {
+    const SF v = a.src_f[(size_t)i * a.pstride_f + (size_t)y * a.W + x];
+    if constexpr (std::is_same_v<SF, float>) return v;
+    else if constexpr (SCALED) return to_f<SF>(v) * a.c.inv_sf;
+    else return to_f<SF>(v);
+  };
+  float d[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    if (i > 0 && (bits & (1u << (i - 1)))) d[i] = ld(opp_of(i), yn, 0);
+    else if (ex_of(i) > 0) d[i] = 0.0f;
+    else d[i] = ld(i, wrap(yn - ey_of(i), a.H), -ex_of(i));
+  }
+  return dev_inlet_drho(d, (float)a.inlet_ux[yn], a.side_in[yn], a.side_in[2 * a.H + yn]);
+}
+
+// The strip on the split ring (NS == 4).  Row r of the strip's ring rows
+// y0-2 .. y1+1 uses slot (r - first) & 3; its g half (g_0 and the eight g_i
+// planes, needed by psi of rows r-1 .. r+1) and its f half (needed by the f
+// pull of rows r-1 .. r+1) complete on separate mbarriers, so each half is
+// refilled as soon as it is no longer read: the g half of row y+4 and the f
+// half of row y+2 are issued at the barrier of row y, 1.5 and 1 rows ahead of
+// their first use.  The mask row of r (needed up to the f pull of row r)
+// arrives with the g half into mask-ring row (r - first) & 7.  The f half of
+// row y0-2 is never needed (the inlet corners read global memory), so the
+// prologue fills f rows y0-1 .. y0+2.
+template <typename SF, int NT, bool SCALED, bool STOCH>
+__device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, int band, int strip, char* smem,
+                                                unsigned& phase, bool& ok) {
+  using L = SlotLayout<SF, NT>;
+  using M = TmaSmem<SF, NT, 4>;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
+  float* psi_ring = reinterpret_cast<float*>(smem + M::OFF_PSI);
+
+  const int t = threadIdx.x;
+  const int x0 = band * NT;
+  const int y0 = strip * a.R, y1 = min(y0 + a.R, a.H);
+  const int x = x0 + t;
+  const bool owned = x < a.W;
+  const bool walls = a.variant == FD_VARIANT_WALLS;
+  const int first = y0 - 2, last = y1 + 1;  // g rows y0-2 .. y1+1, f rows y0-1 .. y1
+  const int hl = (t == NT / 2) ? -1 : (t == NT - 1 ? NT : 0);
+  const bool halo = (t == NT / 2) || (t == NT - 1);
+
+  auto slot = [&](int r) { return M::OFF_SLOT + ((r - first) & 3) * M::SLOT; };
+  auto mrow = [&](int r) { return M::OFF_MASK + ((r - first) & 7) * L::RM; };
+  // parity bits of the fills issued (thread 0), for the error path
+  unsigned issued = phase;
+  auto issue_g = [&](int r) {
+    if (r > last || !ok) return;
+    const int b = (r - first) & 3;
+    issue_g_half<SF, NT>(a, smem + slot(r), smem + mrow(r), &bars[b], r, x0);
+    issued ^= 1u << b;
+  };
+  auto issue_f = [&](int r) {
+    if (r > y1 || !ok) return;
+    const int b = 4 + ((r - first) & 3);
+    issue_f_half<SF, NT>(a, smem + slot(r), &bars[b], r, x0);
+    issued ^= 1u << b;
+  };
+  auto wait_bar = [&](int b) {
+    if (ok) ok = mbar_wait(&bars[b], (phase >> b) & 1u);
+    phase ^= 1u << b;
+  };
+  auto wait_g = [&](int r) { wait_bar((r - first) & 3); };
+  auto wait_f = [&](int r) { wait_bar(4 + ((r - first) & 3)); };
+
+  if (t == 0) {
+    for (int r = first; r < first + 4; ++r) issue_g(r);
+    for (int r = y0 - 1; r < y0 + 3; ++r) issue_f(r);
+  }
+  int pslot = 0;  // psi ring slot of row y0-1; rows y0-1, y0, y0+1 use pslot, +1, +2 (mod 4)
+  auto psi_row = [&](int k) { return psi_ring + ((pslot + k) & 3) * M::PSI_ROW; };
+  // psi of ring row r (this thread's cell and its halo cell) into psi ring row k
+  float gN[9];
+  auto psi_of_row = [&](int r, int k) {
+    const int rows[3] = {slot(r - 1), slot(r), slot(r + 1)};
+    const bool ghost = walls && (r < 0 || r >= a.H);
+    const int yr = wrap(r, a.H);
+    float* pr = psi_row(k);
+    const float pv = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(r), x, t, yr, gN);
+    pr[t + 1] = pv;
+    if (halo) {
+      float gh[9];
+      pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(r), x0 + hl, hl, yr, gh);
+    }
+    return pv;
+  };
+
+  // prologue: psi of rows y0-1 and y0; the g halves of rows y0-2 and y0-1
+  // are refilled (rows y0+2, y0+3) as soon as each is done
+  wait_g(y0 - 2);
+  wait_g(y0 - 1);
+  wait_g(y0);
+  float pS = psi_of_row(y0 - 1, 0);  // psi of this column at rows y-1 and y
+  __syncthreads();
+  if (t == 0) issue_g(y0 + 2);
+  wait_g(y0 + 1);
+  float pC = psi_of_row(y0, 1);
+  float gC[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) gC[i] = gN[i];
+  __syncthreads();
+  if (t == 0) issue_g(y0 + 3);
+  wait_f(y0 - 1);
+  wait_f(y0);
+
+  for (int y = y0; y < y1; ++y) {
+    // 1. psi of row y+1 from the g halves of rows y, y+1, y+2
+    wait_g(y + 2);
+    const float pN = psi_of_row(y + 1, 2);
+    float drho_nb = 0.0f;
+    if (walls && x == 0 && (y == 0 || y == a.H - 1)) drho_nb = inlet_corner_drho<SF, SCALED>(a, y == 0 ? 1 : a.H - 2);
+    // 2. psi(y+1) complete: the g half of row y and the f half of row y-2 are
+    //    free (the f half of row y0+2 was filled by the prologue)
+    __syncthreads();
+    if (t == 0) {
+      issue_g(y + 4);
+      if (y > y0) issue_f(y + 2);
+    }
+    wait_f(y + 1);
+    // 3. stencils, f pull, Zou-He, collision, store
+    if (owned) {
+      const float* pm = psi_row(0);
+      const float* pc = psi_row(1);
+      const float* pn = psi_row(2);
+      const int j = t + 1;
+      const float C = pC, E = pc[j + 1], Wv = pc[j - 1], N = pN, S = pS;
+      const float NE = pn[j + 1], NW = pn[j - 1], SE = pm[j + 1], SW = pm[j - 1];
+      const float gx = (4.0f * (E - Wv) + ((NE - NW) + (SE - SW))) * (1.0f / 12.0f);
+      const float gy = (4.0f * (N - S) + ((NE + NW) - (SE + SW))) * (1.0f / 12.0f);
+      const float lap = (4.0f * ((N + S) + (E + Wv)) + ((NE + NW) + (SE + SW)) - 20.0f * C) * (1.0f / 6.0f);
+      const int rows[3] = {slot(y - 1), slot(y), slot(y + 1)};
+      const unsigned m = mask_at<SF, NT>(smem, mrow(y), t);
+      float f[9];
+      pull_cell<SF, NT, false, SCALED>(smem, a.c, rows, t, m & 0xFFu, f);
+      if (x == 0 || x == a.W - 1) {
+        const int o = (x == 0) ? 0 : 3;
+        dev_zou_he_f(a.c, a.variant, a.H, a.W, x, y, f, (float)a.inlet_ux[y], a.side_in[(o + 0) * a.H + y],
+                     a.side_in[(o + 1) * a.H + y], a.side_in[(o + 2) * a.H + y], drho_nb);
+        a.side_out[(o + 0) * a.H + y] = gx;
+        a.side_out[(o + 1) * a.H + y] = gy;
+        a.side_out[(o + 2) * a.H + y] = a.c.a * C * (1.0f - C * C) - a.c.kappa * lap;
+      }
+      if (!(m & SOLID)) {
+        const DevMacro mc = dev_macros(a.c, f, C, gx, gy, lap);
+        dev_collide(a.c, mc, f, gC);
+      }
+      const size_t q = (size_t)y * a.W + x;
+      uint32_t rs = 0;  // stochastic rounding state of this cell (fd_dev.cuh)
+      if constexpr (STOCH) rs = sr_hash((uint32_t)q ^ a.seed);
+      auto put = [&](SF* p, float v, float scale) {
+        if constexpr (std::is_same_v<SF, float>) {
+          *p = v;
+        } else {
+          if constexpr (SCALED) v *= scale;
+          if constexpr (STOCH) {
+            rs = sr_next(rs);
+            *p = from_f_sr<SF>(v, rs);
+          } else {
+            *p = from_f<SF>(v);
+          }
+        }
+      };
+      SF* pf = a.dst_f + q;
+#pragma unroll
+      for (int i = 0; i < 9; ++i, pf += a.pstride_f) put(pf, f[i], a.c.sf);
+      a.dst_g0[q] = gC[0];
+      SF* pg = a.dst_gi + q;
+#pragma unroll
+      for (int i = 1; i < 9; ++i, pg += a.pstride_f) put(pg, gC[i], a.c.sg);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) gC[i] = gN[i];
+    pS = pC;
+    pC = pN;
+    pslot = (pslot + 1) & 3;
+  }
+  // After a wait gave up no further copies were issued; make sure the last
+  // copy issued on every mbarrier has landed (bounded) before the ring is
+  // reused or released.
+  if (!ok && t == 0) {
+    for (int b = 0; b < M::NBAR; ++b) mbar_wait(&bars[b], ((issued >> b) & 1u) ^ 1u);
+  }
+  ok = __syncthreads_and(ok);
+}
+
+template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
+__device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int strip, char* smem, unsigned& phase,
+                                          bool& ok) {
+  if constexpr (NS == 4) tma_strip_split<SF, NT, SCALED, STOCH>(a, band, strip, smem, phase, ok);
+  else tma_strip_ring<SF, NT, NS, SCALED, STOCH>(a, band, strip, smem, phase, ok);
+}
+
 template <typename SF, int NT, int NS>
 __device__ __forceinline__ void init_ring(char* smem) {
   using M = TmaSmem<SF, NT, NS>;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
   if (threadIdx.x == 0) {
-    for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < M::NBAR; ++s) mbar_init(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
