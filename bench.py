@@ -15,7 +15,8 @@ with the state resident in HBM (18 planes x 8.4 M cells x 4 B = 604 MB read
 and written per step, far larger than L2, so no L2 flush is needed).  `e2e`
 is the same metric through the host-buffer API: every step uploads the
 populations from pinned host memory, advances one iteration and downloads
-them again.  With --gpus N > 1 each rank runs its own instance (replicas,
+them again (fd_fused_step_packed_host: the two copy directions and the
+kernel pipelined over row chunks).  With --gpus N > 1 each rank runs its own instance (replicas,
 weak scaling, no collective on the data path).
 
 --impl reference times the CPU implementation of the same step (the numpy
@@ -276,25 +277,32 @@ def run_ours(args):
     finite = bool(torch.isfinite(lat.psi).all().item())
     lat.enter_fused()
 
-    # end to end through the host-buffer API: populations in from pinned host
-    # memory, one iteration, populations back out
+    # end to end through the host-buffer API: the state in pinned host memory,
+    # every step uploaded, advanced one iteration and downloaded again (packed
+    # storage: one pipelined fd_fused_step_packed_host call per step; FP64:
+    # upload, fused step, download)
     state = lat.current_buffer()
     e2e_steps = max(3, min(args.steps, 20))
     e2e_s = float("nan")
+
+    def host_step(host):
+        if lat.storage is not None:
+            lat.advance_host(host)
+        else:
+            lat.upload_populations(host)
+            lat.advance(1, args.rows)
+            lat.download_populations(host)
+
     if not args.no_e2e:
         host = torch.empty(state.shape, dtype=state.dtype, pin_memory=True)
         host.copy_(state)
         for _ in range(2):
-            lat.upload_populations(host)
-            lat.advance(1, args.rows)
-            lat.download_populations(host)
+            host_step(host)
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            lat.upload_populations(host)
-            lat.advance(1, args.rows)
-            lat.download_populations(host)
+            host_step(host)
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
 

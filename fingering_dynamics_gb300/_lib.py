@@ -88,8 +88,9 @@ SIGNATURES = {
     "fd_unpack": [_P, _S, _VP, _I, _VP, _VP],
     "fd_fused_step_packed": [_P, _S, _VP, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
     "fd_device_status": [C.POINTER(C.c_uint), _I],
-    "fd_selftest_wait_timeout": [C.c_uint, _VP],
+    "fd_selftest_wait_timeout": [C.c_uint, _I, _VP],
     "fd_fused_step_packed_noalloc": [_P, _S, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
+    "fd_fused_step_packed_host": [_P, _S, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP],
     "fd_diag_scratch_bytes": [],
     "fd_batch_create": [C.POINTER(fd_instance), _I, _S, _I, _I, C.POINTER(C.c_void_p)],
     "fd_batch_configure": [_VP, _I, _I],

@@ -38,6 +38,7 @@ UNITS = {
     "fd_noalloc.cu": [],
     "fd_diag.cu": [],
     "fd_batch.cu": [],
+    "fd_host_step.cu": [],
     "sg_kernels.cu": [],
     "sg_tcgen05.cu": [],
 }

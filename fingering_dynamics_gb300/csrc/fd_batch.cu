@@ -256,3 +256,25 @@ int fd_batch_destroy(fd_batch* b) {
 }
 
 }  // extern "C"
+
+namespace fd {
+
+// This unit's copy of the device error word (fd_fused_tma.cuh), which the
+// batched kernel latches; fd_device_status() combines it with the others.
+int batch_device_error(unsigned* out, bool clear) { return device_error_word(out, clear); }
+
+// The failure path of the bounded wait, on this unit's error word: one thread
+// waits on an mbarrier that nothing arrives on and gives up after `polls`.
+__global__ void k_selftest_wait_timeout_batch(unsigned polls) {
+  __shared__ uint64_t bar;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  mbar_wait(&bar, 0u, polls);
+}
+
+int batch_selftest_wait_timeout(unsigned polls, cudaStream_t s) {
+  k_selftest_wait_timeout_batch<<<1, 1, 0, s>>>(polls);
+  return FD_OK;
+}
+
+}  // namespace fd

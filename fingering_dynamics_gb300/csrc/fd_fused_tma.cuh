@@ -54,9 +54,22 @@ constexpr int tma_ring_depth() {
 }
 
 // Device-side error word: bit 0 = an mbarrier wait gave up (copy never
-// completed).  Read and cleared by fd_device_status().  This header is
-// included by exactly one translation unit.
+// completed).  The library is built without relocatable device code, so every
+// translation unit that includes this header has its own copy, read and
+// cleared through its own device_error_word(); fd_device_status() combines
+// the copies of all units.
 __device__ unsigned int g_fd_device_error = 0;
+
+namespace {
+inline int device_error_word(unsigned* out, bool clear) {
+  if (cudaMemcpyFromSymbol(out, g_fd_device_error, sizeof(unsigned)) != cudaSuccess) return FD_ERR_CUDA;
+  if (clear) {
+    const unsigned zero = 0;
+    if (cudaMemcpyToSymbol(g_fd_device_error, &zero, sizeof(unsigned)) != cudaSuccess) return FD_ERR_CUDA;
+  }
+  return FD_OK;
+}
+}  // namespace
 
 constexpr unsigned kWaitLimit = 1u << 24;  // bounded spins on an mbarrier
 
@@ -649,13 +662,15 @@ __device__ __forceinline__ void init_ring(char* smem) {
   __syncthreads();
 }
 
+// CTA b takes band b % nbands of strip strip0 + b / nbands.
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
-__global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nbands) {
+__global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nbands, int strip0) {
   extern __shared__ __align__(128) char smem[];
   init_ring<SF, NT, NS>(smem);
   unsigned phase = 0;
   bool ok = true;
-  tma_strip<SF, NT, NS, SCALED, STOCH>(a, (int)blockIdx.x % nbands, (int)blockIdx.x / nbands, smem, phase, ok);
+  tma_strip<SF, NT, NS, SCALED, STOCH>(a, (int)blockIdx.x % nbands, strip0 + (int)blockIdx.x / nbands, smem, phase,
+                                       ok);
 }
 
 // One lattice of a batch: its arguments for both ping-pong parities.
@@ -702,13 +717,18 @@ __global__ void __launch_bounds__(NT) k_fused_tma_batch(const BatchInst<SF>* __r
 
 namespace fd {
 
+// Raise the kernel's dynamic shared-memory limit (once per device).
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
-int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, char* pa,
-                     char* pb, float* sa, float* sb, int nsteps, int R, uint32_t seed, cudaStream_t st) {
-  using M = TmaSmem<SF, NT, NS>;
+cudaError_t tma_prepare_kernel() {
   static std::atomic<unsigned long long> attr_done{0};
-  if (ensure_smem_attr(k_fused_tma<SF, NT, NS, SCALED, STOCH>, M::BYTES, attr_done) != cudaSuccess)
-    return FD_ERR_CUDA;
+  return ensure_smem_attr(k_fused_tma<SF, NT, NS, SCALED, STOCH>, TmaSmem<SF, NT, NS>::BYTES, attr_done);
+}
+
+// Arguments of the staged kernel for one lattice with strips of R rows (R <= 0:
+// about two waves of CTAs); the buffers are set per step by tma_set_step.
+template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
+DevArgs<SF> tma_args(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, int R) {
+  using M = TmaSmem<SF, NT, NS>;
   const PackedLayout<SF> L = packed_layout<SF>(p.H, p.W);
   DevArgs<SF> a;
   a.c = c;
@@ -722,6 +742,7 @@ int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask,
   const int nbands = (p.W + NT - 1) / NT;
   if (R <= 0) {
     int per_sm = 1;
+    tma_prepare_kernel<SF, NT, NS, SCALED, STOCH>();  // the occupancy depends on the raised limit
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tma<SF, NT, NS, SCALED, STOCH>, NT, M::BYTES);
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
@@ -730,25 +751,49 @@ int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask,
     long long strips = (want + nbands - 1) / nbands;
     R = (int)((p.H + strips - 1) / strips);
     if (R < 16) R = 16;
-    if (R > p.H) R = p.H;
   }
+  if (R > p.H) R = p.H;
   a.R = R;
   a.nstrips = (p.H + R - 1) / R;
   a.nchunks = nbands;
-  const unsigned blocks = (unsigned)(nbands * a.nstrips);
+  return a;
+}
+
+// Point the arguments at one step's buffers; `seed` is the step's seed before
+// hashing (the call's seed plus the step index).
+template <typename SF>
+void tma_set_step(DevArgs<SF>& a, const char* src, char* dst, float* side_in, float* side_out, uint32_t seed) {
+  const PackedLayout<SF> L = packed_layout<SF>(a.H, a.W);
+  a.src_f = reinterpret_cast<const SF*>(src + L.off_f);
+  a.src_g0 = reinterpret_cast<const float*>(src + L.off_g0);
+  a.src_gi = reinterpret_cast<const SF*>(src + L.off_gi);
+  a.dst_f = reinterpret_cast<SF*>(dst + L.off_f);
+  a.dst_g0 = reinterpret_cast<float*>(dst + L.off_g0);
+  a.dst_gi = reinterpret_cast<SF*>(dst + L.off_gi);
+  a.side_in = side_in;
+  a.side_out = side_out;
+  a.seed = sr_hash(seed);
+}
+
+// One step over strips strip0 .. strip0 + nstrips - 1 of the lattice.
+template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
+int launch_tma_strips(const DevArgs<SF>& a, int strip0, int nstrips, cudaStream_t st) {
+  using M = TmaSmem<SF, NT, NS>;
+  if (tma_prepare_kernel<SF, NT, NS, SCALED, STOCH>() != cudaSuccess) return FD_ERR_CUDA;
+  if (nstrips <= 0) return FD_OK;
+  const unsigned blocks = (unsigned)(a.nchunks * nstrips);
+  k_fused_tma<SF, NT, NS, SCALED, STOCH><<<blocks, NT, M::BYTES, st>>>(a, a.nchunks, strip0);
+  return FD_OK;
+}
+
+template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
+int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, char* pa,
+                     char* pb, float* sa, float* sb, int nsteps, int R, uint32_t seed, cudaStream_t st) {
+  DevArgs<SF> a = tma_args<SF, NT, NS, SCALED, STOCH>(p, c, mask, inlet_ux, R);
   for (int s = 0; s < nsteps; ++s) {
-    char* src = (s % 2 == 0) ? pa : pb;
-    char* dst = (s % 2 == 0) ? pb : pa;
-    a.src_f = reinterpret_cast<const SF*>(src + L.off_f);
-    a.src_g0 = reinterpret_cast<const float*>(src + L.off_g0);
-    a.src_gi = reinterpret_cast<const SF*>(src + L.off_gi);
-    a.dst_f = reinterpret_cast<SF*>(dst + L.off_f);
-    a.dst_g0 = reinterpret_cast<float*>(dst + L.off_g0);
-    a.dst_gi = reinterpret_cast<SF*>(dst + L.off_gi);
-    a.side_in = (s % 2 == 0) ? sa : sb;
-    a.side_out = (s % 2 == 0) ? sb : sa;
-    a.seed = sr_hash(seed + (uint32_t)s);
-    k_fused_tma<SF, NT, NS, SCALED, STOCH><<<blocks, NT, M::BYTES, st>>>(a, nbands);
+    const bool even = s % 2 == 0;
+    tma_set_step(a, even ? pa : pb, even ? pb : pa, even ? sa : sb, even ? sb : sa, seed + (uint32_t)s);
+    if (int r = launch_tma_strips<SF, NT, NS, SCALED, STOCH>(a, 0, a.nstrips, st)) return r;
   }
   return cudaGetLastError() == cudaSuccess ? FD_OK : FD_ERR_CUDA;
 }

@@ -214,6 +214,37 @@ class Lattice:
             self.scur = 1 - self.scur
         self.iteration += n
 
+    def advance_host(self, host_in: torch.Tensor, host_out: torch.Tensor | None = None, n: int = 1,
+                     chunk_rows: int = 0):
+        """n fused iterations of a state held in host memory: ``host_in`` holds
+        the packed bytes of :meth:`current_buffer` (as written by
+        :meth:`download_populations`); they are uploaded, advanced and the
+        result downloaded into ``host_out`` (default ``host_in``, in place) by
+        one pipelined call (fd_fused_step_packed_host), the copies of both
+        directions overlapping each other and the kernels.  The device state
+        follows as after :meth:`advance`.  Asynchronous on the lattice's
+        stream; pinned host tensors are needed for the overlap."""
+        self._require("fused")
+        if self.storage is None:
+            raise ValueError("advance_host needs packed storage (dtype f32, f16 or bf16)")
+        if n <= 0:
+            return
+        host_out = host_in if host_out is None else host_out
+        nbytes = self.ppop[self.pcur].numel()
+        for t in (host_in, host_out):
+            if t.device.type != "cpu" or t.dtype != torch.uint8 or t.numel() != nbytes or not t.is_contiguous():
+                raise ValueError(f"host buffers must be contiguous uint8 CPU tensors of {nbytes} bytes")
+        a, b = self.ppop[self.pcur], self.ppop[1 - self.pcur]
+        sa, sb = self.side[self.scur], self.side[1 - self.scur]
+        self.storage.seed = self.step_seed()
+        L.call("fd_fused_step_packed_host", C.byref(self.prm), C.byref(self.storage), _ptr(self.mask),
+               _ptr(self.inlet_ux), _ptr(host_in), _ptr(host_out), _ptr(a), _ptr(b), _ptr(sa), _ptr(sb), int(n),
+               int(chunk_rows), self._stream())
+        if n % 2:
+            self.pcur = 1 - self.pcur
+            self.scur = 1 - self.scur
+        self.iteration += n
+
     def peek(self):
         """Fields of the next iteration (psi, rho, ux, uy, ... in the field
         tensors) without leaving fused mode: the pending packed state is

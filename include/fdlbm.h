@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define FDLBM_ABI_VERSION 3
+#define FDLBM_ABI_VERSION 4
 
 enum fd_status {
   FD_OK = 0,
@@ -265,6 +265,27 @@ int fd_fused_step_packed_noalloc(const fd_params* prm, const fd_storage* st, con
                                  const double* inlet_ux, void* pop_a, void* pop_b, void* side, int nsteps,
                                  int rows_per_warp, void* stream);
 
+/* The step for a caller whose state lives in HOST memory, as the reference's
+ * numpy arrays do (its loop body, fingering_periodic.py:454-479 /
+ * fingering.py:558-585, on arrays it owns): the packed state in `host_in`
+ * (fd_packed_bytes(), the device layout) is uploaded into pop_a, advanced
+ * nsteps (>= 1) iterations as fd_fused_step_packed would (same results bit for
+ * bit, same seeds), and the result is downloaded into `host_out`.  side_a
+ * holds the boundary values of the state on entry (device, 6*H floats, as for
+ * fd_fused_step_packed); the device state after the call is in pop_b / side_b
+ * when nsteps is odd, else in pop_a / side_a.  The upload, the first and last
+ * iterations and the download are pipelined over chunks of about chunk_rows
+ * rows (<= 0: about 16 chunks; rounded to whole strips of 16 rows): both copy
+ * directions run at once and the kernels run under them.  host_in may equal
+ * host_out.  Host buffers should be pinned (cudaHostAlloc / cudaHostRegister),
+ * or the copies do not overlap.  W must be a multiple of 8.  Asynchronous on
+ * `stream` like every step; uses two internal streams per device, and calls on
+ * one device from several host threads serialise while they enqueue.  No
+ * counterpart in the reference (its state never leaves host memory). */
+int fd_fused_step_packed_host(const fd_params* prm, const fd_storage* st, const uint16_t* mask,
+                              const double* inlet_ux, const void* host_in, void* host_out, void* pop_a,
+                              void* pop_b, void* side_a, void* side_b, int nsteps, int chunk_rows, void* stream);
+
 /* ---- batched ensemble ----------------------------------------------------- */
 
 /* One member of a batch: its parameters and its packed buffers (as for
@@ -336,13 +357,15 @@ int fd_diagnostics(const fd_params* prm, int dtype, const fd_storage* st, const 
 /* Self-test of the failure path: one thread waits, through the staged kernel's
  * bounded mbarrier wait, on a barrier that nothing arrives on; after `polls`
  * polls (1 .. 2^20) the wait gives up and bit 0 of the device error word is set
- * (read with fd_device_status).  Faults, traps and hangs nothing.  No
- * counterpart in the reference. */
-int fd_selftest_wait_timeout(unsigned polls, void* stream);
+ * (read with fd_device_status).  unit 0 runs it in the code unit of the
+ * single-lattice kernels, unit 1 in that of the batched kernel (each unit of
+ * the library has its own copy of the word).  Faults, traps and hangs nothing.
+ * No counterpart in the reference. */
+int fd_selftest_wait_timeout(unsigned polls, int unit, void* stream);
 
 /* Device-side status word of the library's kernels (bit 0: a bounded wait on
- * an asynchronous copy gave up).  Copies it to *out and, if clear != 0,
- * resets it.  Synchronous.  No counterpart in the reference (numpy raises
+ * an asynchronous copy gave up), the OR over the library's code units.  Copies
+ * it to *out and, if clear != 0, resets it.  Synchronous.  No counterpart in the reference (numpy raises
  * instead, fingering_periodic.py:497). */
 int fd_device_status(unsigned* out, int clear);
 

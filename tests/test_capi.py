@@ -46,7 +46,7 @@ def test_binding_table_matches_headers():
 
 def test_abi_version_and_error_path(lib):
     from fingering_dynamics_gb300 import _lib as L
-    assert L.lib().fd_abi_version() == 3
+    assert L.lib().fd_abi_version() == 4
     # host-side argument checks run without a GPU and report through fd_last_error
     with pytest.raises(L.FDError) as e:
         L.call("fd_fused_step", None, 1, None, None, None, None, None, None, 1, 0, None)

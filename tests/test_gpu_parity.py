@@ -178,17 +178,22 @@ def test_device_status_clean_after_runs():
     assert v.value == 0
 
 
-def test_bounded_wait_gives_up_and_the_context_stays_usable():
+@pytest.mark.parametrize("unit", [0, 1], ids=["single_lattice_unit", "batch_unit"])
+def test_bounded_wait_gives_up_and_the_context_stays_usable(unit):
     """A wait on an mbarrier that nothing arrives on gives up after a short
-    poll limit, latches the status bit, and the next step runs normally."""
+    poll limit, latches the status bit (in the code unit of the single-lattice
+    kernels or in that of the batched kernel: fd_device_status reports both),
+    and the next step runs normally."""
     import ctypes as C
     from fingering_dynamics_gb300 import _lib as L
     v = C.c_uint(0)
     L.call("fd_device_status", C.byref(v), 1)
-    L.call("fd_selftest_wait_timeout", 1000, None)
+    L.call("fd_selftest_wait_timeout", 1000, unit, None)
     torch.cuda.synchronize()
     L.call("fd_device_status", C.byref(v), 1)
     assert v.value & 1
+    L.call("fd_device_status", C.byref(v), 0)
+    assert v.value == 0
     fx = load("walls_rects_24x48")
     lat = make_lattice(fx, "f32")
     lat.step(5)
