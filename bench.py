@@ -337,6 +337,8 @@ def run_ours(args):
                 "h2d_bytes_per_step": pop_bytes, "d2h_bytes_per_step": pop_bytes},
             "gpu_launches": args.steps,
             "clocks": clocks,
+            # fluid cells only (the metric counts every cell, solid ones too, as the reference streams them)
+            "mflups_fluid": round(mlups * g.porosity, 1),
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()

@@ -724,8 +724,13 @@ cudaError_t tma_prepare_kernel() {
   return ensure_smem_attr(k_fused_tma<SF, NT, NS, SCALED, STOCH>, TmaSmem<SF, NT, NS>::BYTES, attr_done);
 }
 
-// Arguments of the staged kernel for one lattice with strips of R rows (R <= 0:
-// about two waves of CTAs); the buffers are set per step by tma_set_step.
+// Arguments of the staged kernel for one lattice with strips of R rows; the
+// buffers are set per step by tma_set_step.  R <= 0 picks the strip count from
+// the resident CTAs per SM (measured on 4096 x 2048): the split ring (FP32,
+// memory-bound) loses up to 8% to a partial last wave and takes the largest
+// count that fits in three full waves (R = 29 there: 36.8 vs 34.0 GLUPS at
+// 3.1 waves); the whole-row ring (FP16/BF16, issue-bound) is best at about two
+// waves, rounded up.
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 DevArgs<SF> tma_args(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, int R) {
   using M = TmaSmem<SF, NT, NS>;
@@ -747,8 +752,9 @@ DevArgs<SF> tma_args(const fd_params& p, const DevCoef& c, const uint16_t* mask,
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long want = 2LL * sms * (per_sm > 0 ? per_sm : 1);  // about two waves
-    long long strips = (want + nbands - 1) / nbands;
+    const long long slots = (long long)sms * (per_sm > 0 ? per_sm : 1);
+    long long strips = M::SPLIT ? 3 * slots / nbands : (2 * slots + nbands - 1) / nbands;
+    if (strips < 1) strips = 1;
     R = (int)((p.H + strips - 1) / strips);
     if (R < 16) R = 16;
   }
