@@ -97,6 +97,7 @@ SIGNATURES = {
     "fd_batch_step": [_VP, _I, _I, _VP],
     "fd_batch_parity": [_VP],
     "fd_batch_tiles": [_VP],
+    "fd_batch_grid": [_VP],
     "fd_batch_destroy": [_VP],
     "fd_diagnostics": [_P, _I, _S, _VP, _VP, _VP, _VP, _VP],
     # learned surrogate (include/fdsurrogate.h)

@@ -2,6 +2,7 @@
 // parameters) advanced together by one persistent launch per iteration over a
 // table of (instance, band, strip) tiles, with the iteration loop replayed
 // from a CUDA graph.
+#include <algorithm>
 #include <vector>
 
 #include "fd_fused_tma.cuh"
@@ -21,7 +22,7 @@ struct fd_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t graph_stream = nullptr;
-  unsigned* d_steps = nullptr;  // two-slot step counter for stochastic rounding (k_fused_tma_batch)
+  unsigned* d_ctl = nullptr;  // step and tile counters, two slots each (k_fused_tma_batch)
 };
 
 namespace fd {
@@ -36,7 +37,9 @@ DevArgs<SF> instance_args(const fd_instance& in, const fd_storage& st, int rows,
   a.H = p.H;
   a.W = p.W;
   a.variant = p.variant;
-  a.R = rows < p.H ? rows : p.H;
+  // strips of equal height (within one row) at most `rows` high
+  const int ns = (p.H + rows - 1) / rows;
+  a.R = (p.H + ns - 1) / ns;
   a.nstrips = (p.H + a.R - 1) / a.R;
   a.nchunks = 0;
   a.P = L.P;
@@ -72,6 +75,15 @@ int prepare(fd_batch* b) {
     for (int s = 0; s < ns; ++s)
       for (int bb = 0; bb < nb; ++bb) tiles.push_back(make_int4(i, bb, s, 0));
   }
+  // largest first (rows of the tile's strip), ties in table order: the
+  // kernel's counter then hands them out greedily
+  auto strip_rows = [&](const int4& t) {
+    const DevArgs<SF>& a = hi[t.x].args[0];
+    const int y0 = t.z * a.R;
+    return (y0 + a.R < a.H ? y0 + a.R : a.H) - y0;
+  };
+  std::stable_sort(tiles.begin(), tiles.end(),
+                   [&](const int4& u, const int4& v) { return strip_rows(u) > strip_rows(v); });
   cudaFree(b->d_inst);
   cudaFree(b->d_tiles);
   b->d_inst = nullptr;
@@ -97,7 +109,7 @@ template <typename SF, int NT, bool STOCH>
 void launch_one(const fd_batch* b, int parity, cudaStream_t st) {
   using M = TmaSmem<SF, NT, tma_ring_depth<SF>()>;
   k_fused_tma_batch<SF, NT, tma_ring_depth<SF>(), false, STOCH><<<b->grid, NT, M::BYTES, st>>>(
-      (const BatchInst<SF>*)b->d_inst, b->d_tiles, b->ntiles, parity, b->d_steps);
+      (const BatchInst<SF>*)b->d_inst, b->d_tiles, b->ntiles, parity, b->d_ctl);
 }
 
 template <typename SF, bool STOCH>
@@ -185,8 +197,8 @@ int fd_batch_create(const fd_instance* inst, int n, const fd_storage* st, int ro
   b->band = band_width;
   b->rows = rows_per_strip;
   b->inst.assign(inst, inst + n);
-  if (cudaMalloc(&b->d_steps, 2 * sizeof(unsigned)) != cudaSuccess ||
-      cudaMemset(b->d_steps, 0, 2 * sizeof(unsigned)) != cudaSuccess) {
+  if (cudaMalloc(&b->d_ctl, 4 * sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(b->d_ctl, 0, 4 * sizeof(unsigned)) != cudaSuccess) {
     const int r = check_launch("fd_batch_create: step counter");
     fd_batch_destroy(b);
     return r;
@@ -245,12 +257,14 @@ int fd_batch_parity(const fd_batch* b) { return b ? b->parity : -1; }
 
 int fd_batch_tiles(const fd_batch* b) { return b ? b->ntiles : -1; }
 
+int fd_batch_grid(const fd_batch* b) { return b ? b->grid : -1; }
+
 int fd_batch_destroy(fd_batch* b) {
   if (!b) return FD_OK;
   drop_graph(b);
   cudaFree(b->d_inst);
   cudaFree(b->d_tiles);
-  cudaFree(b->d_steps);
+  cudaFree(b->d_ctl);
   delete b;
   return FD_OK;
 }

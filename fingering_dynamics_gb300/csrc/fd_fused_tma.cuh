@@ -679,36 +679,47 @@ struct BatchInst {
   DevArgs<SF> args[2];
 };
 
-// Persistent kernel over a tile table of (instance, band, strip) entries: CTA
-// b takes tiles b, b + gridDim.x, ...  Every instance advances one iteration.
+// Persistent kernel over a tile table of (instance, band, strip) entries,
+// largest tiles first: each CTA takes the next untaken tile from a counter
+// until none is left (greedy largest-first balancing of uneven tiles).  Every
+// instance advances one iteration.
 //
-// Step counter for stochastic rounding: `steps` holds two slots; the launch of
-// parity p reads slot p (the number of batch steps done so far) and one
-// thread writes slot 1-p = slot p + 1 for the next launch.  A launch never
-// writes the slot it reads, and launches on a stream are ordered, so the
-// sequence is deterministic and advances under CUDA-graph replay too.  A
-// member's step seed is its own seed (args.seed) plus the counter.
+// `ctl` holds two two-slot counters, written so that the launch of parity p
+// never writes a slot it reads and launches on a stream are ordered (the
+// sequence is deterministic and advances under CUDA-graph replay too):
+//   ctl[0..1]  batch steps done, for stochastic rounding: the launch reads
+//              ctl[p] and one thread writes ctl[1-p] = ctl[p] + 1; a member's
+//              step seed is its own seed (args.seed) plus the count;
+//   ctl[2..3]  tile counter: the launch takes tiles from ctl[2+p] and one
+//              thread zeroes ctl[2+(1-p)] for the next launch.
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 __global__ void __launch_bounds__(NT) k_fused_tma_batch(const BatchInst<SF>* __restrict__ inst,
                                                         const int4* __restrict__ tiles, int ntiles, int parity,
-                                                        unsigned* __restrict__ steps) {
+                                                        unsigned* __restrict__ ctl) {
   extern __shared__ __align__(128) char smem[];
   __shared__ DevArgs<SF> sa;
+  __shared__ int next;
   init_ring<SF, NT, NS>(smem);
   unsigned done = 0;
-  if constexpr (STOCH) {
-    done = steps[parity];
-    if (blockIdx.x == 0 && threadIdx.x == 0) steps[parity ^ 1] = done + 1;
+  if constexpr (STOCH) done = ctl[parity];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if constexpr (STOCH) ctl[parity ^ 1] = done + 1;
+    ctl[2 + (parity ^ 1)] = 0;
   }
   unsigned phase = 0;
   bool ok = true;
-  for (int k = blockIdx.x; k < ntiles && ok; k += gridDim.x) {
-    const int4 tl = tiles[k];
+  for (;;) {
     if (threadIdx.x == 0) {
-      sa = inst[tl.x].args[parity];
-      if constexpr (STOCH) sa.seed = sr_hash(sa.seed + done);
+      next = (int)atomicAdd(&ctl[2 + parity], 1u);
+      if (next < ntiles) {
+        sa = inst[tiles[next].x].args[parity];
+        if constexpr (STOCH) sa.seed = sr_hash(sa.seed + done);
+      }
     }
     __syncthreads();
+    const int k = next;
+    if (k >= ntiles || !ok) break;
+    const int4 tl = tiles[k];
     tma_strip<SF, NT, NS, SCALED, STOCH>(sa, tl.y, tl.z, smem, phase, ok);
   }
 }

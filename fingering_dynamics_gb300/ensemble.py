@@ -182,9 +182,42 @@ class Ensemble:
             lat.iteration += n
         return e0.elapsed_time(e1) / 1e3
 
-    def autotune(self, candidates=DEFAULT_CANDIDATES, steps: int = 20) -> dict:
+    def tiles_for(self, band_width: int, rows_per_strip: int) -> int:
+        """Tiles per iteration of the shape (as fd_batch builds them)."""
+        return sum(-(-lat.W // band_width) * -(-lat.H // min(rows_per_strip, lat.H)) for lat in self.lattices)
+
+    def wave_candidates(self, bands=(64, 128, 256), max_rounds: int = 8, min_fill: float = 0.9) -> list:
+        """Shapes whose tile count just fits a whole number of rounds of the
+        persistent grid (every CTA takes one tile at a time): for each band
+        width and round count r, the shortest strips whose tiles fit in r
+        rounds, kept when they fill at least `min_fill` of them.  A tile count
+        just over a whole number of rounds leaves a last round in which a few
+        CTAs run while the others wait (up to a fifth of the launch)."""
+        keep = self.config
+        out = []
+        hmax = max(lat.H for lat in self.lattices)
+        for band in bands:
+            self.configure(band, 64)
+            grid = int(L.lib().fd_batch_grid(self._batch))
+            if grid <= 0:
+                continue
+            for r in range(1, max_rounds + 1):
+                rows = next((h for h in range(16, hmax + 1) if self.tiles_for(band, h) <= r * grid), None)
+                if rows is None:
+                    continue
+                t = self.tiles_for(band, rows)
+                if t > (r - 1) * grid and t >= min_fill * r * grid:
+                    out.append((band, rows))
+        if keep is not None:
+            self.configure(*keep)
+        return sorted(set(out))
+
+    def autotune(self, candidates=None, steps: int = 20) -> dict:
         """Time every (band width, rows per strip) candidate on this ensemble
-        and keep the fastest; returns {candidate: MLUPS}."""
+        and keep the fastest; returns {candidate: MLUPS}.  Default candidates:
+        a fixed set plus the shapes that fill whole rounds of the grid."""
+        if candidates is None:
+            candidates = sorted(set(DEFAULT_CANDIDATES) | set(self.wave_candidates()))
         res = {}
         for band, rows in candidates:
             self.configure(band, rows)

@@ -308,7 +308,8 @@ typedef struct fd_batch fd_batch;
 /* Build a batch over n members sharing one packed storage type (unscaled).
  * Every iteration is one persistent launch of the staged kernel over a table
  * of (member, band, strip) tiles: bands of band_width cells (64, 128, 256) and
- * strips of rows_per_strip rows.  Allocates the (small) device tables. */
+ * strips of at most rows_per_strip rows (a member's strips are of equal
+ * height within one row).  Allocates the (small) device tables. */
 int fd_batch_create(const fd_instance* inst, int n, const fd_storage* st, int rows_per_strip, int band_width,
                     fd_batch** out);
 
@@ -325,6 +326,12 @@ int fd_batch_parity(const fd_batch* b);
 
 /* Number of tiles per iteration. */
 int fd_batch_tiles(const fd_batch* b);
+
+/* CTAs of the persistent launch (resident CTAs per SM x SMs, at most the tile
+ * count).  The CTAs take tiles from a counter, tallest strips first; a tile
+ * count just under a whole number of rounds of the grid avoids a last round in
+ * which a few CTAs run while the rest wait. */
+int fd_batch_grid(const fd_batch* b);
 
 int fd_batch_destroy(fd_batch* b);
 

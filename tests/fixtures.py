@@ -76,3 +76,16 @@ def oracle_fields(st):
     for n in ("rho", "ux", "uy", "p", "mu", "mix_tau"):
         out[n] = st.full(n)
     return out
+
+
+def packed_planes(buf, H, W, dtype):
+    """The 18 planes of a packed state buffer (a uint8 tensor) without the
+    padding that rounds each plane up to 256 bytes, which nothing writes."""
+    import torch
+    es = 4 if dtype == "f32" else 2
+    P = H * W
+    bf, bg = (P * es + 255) // 256 * 256, (P * 4 + 255) // 256 * 256
+    parts = [buf[i * bf:i * bf + P * es] for i in range(9)]
+    parts.append(buf[9 * bf:9 * bf + P * 4])
+    parts += [buf[9 * bf + bg + i * bf:9 * bf + bg + i * bf + P * es] for i in range(8)]
+    return torch.cat([p.cpu() for p in parts])

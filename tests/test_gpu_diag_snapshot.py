@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from fixtures import load, oracle_from_fixture
+from fixtures import load, oracle_from_fixture, packed_planes
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -70,7 +70,11 @@ def test_snapshot_resume_bitwise(dtype, tmp_path):
     b.load_snapshot(str(tmp_path / "s.npz"))
     b.advance(5)
     assert b.iteration == straight.iteration
-    assert torch.equal(b.current_buffer(), straight.current_buffer())
+    if dtype == "f64":
+        assert torch.equal(b.current_buffer(), straight.current_buffer())
+    else:  # packed: compare the planes, not the padding between them
+        assert torch.equal(packed_planes(b.current_buffer(), b.H, b.W, dtype),
+                           packed_planes(straight.current_buffer(), b.H, b.W, dtype))
     # reference-mode snapshot
     straight.exit_fused()
     c = _lattice(name, dtype)

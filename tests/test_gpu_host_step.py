@@ -7,6 +7,8 @@ several chunk sizes, in place and into a separate buffer, over repeated calls.
 """
 import pytest
 
+from fixtures import packed_planes as planes
+
 pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
@@ -35,19 +37,6 @@ def pair(variant, H, W, dtype, rounding="stochastic"):
         lat.enter_fused()
         out.append(lat)
     return out
-
-
-def planes(buf, H, W, dtype):
-    """The 18 planes of a packed buffer without the padding that rounds each
-    plane up to 256 bytes (nothing writes the padding)."""
-    es = 4 if dtype == "f32" else 2
-    rnd = lambda n: (n + 255) // 256 * 256  # noqa: E731
-    P = H * W
-    bf, bg = rnd(P * es), rnd(P * 4)
-    parts = [buf[i * bf:i * bf + P * es] for i in range(9)]
-    parts.append(buf[9 * bf:9 * bf + P * 4])
-    parts += [buf[9 * bf + bg + i * bf:9 * bf + bg + i * bf + P * es] for i in range(8)]
-    return torch.cat([p.cpu() for p in parts])
 
 
 def pinned_copy(t):
