@@ -10,9 +10,13 @@
 //   download stream : chunk c device -> host once it is computed
 //
 // so the two copy directions run at the same time and the kernel runs under
-// them.  A chunk is a whole number of strips of the staged kernel; every cell
-// is computed exactly as by fd_fused_step_packed (strips only schedule the
-// work), so the results are identical.
+// them.  The download stream is the slower one and cannot start before chunks
+// 0..2 have landed and chunk 1 is computed, so the first chunks are small
+// (1, 1, 2, 4 strips) and the rest about 1/16 of the lattice.  A chunk is a
+// whole number of strips of the staged kernel; every cell is computed exactly
+// as by fd_fused_step_packed (strips only schedule the work), so the results
+// are identical.
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -121,14 +125,19 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
   const int H = prm->H, W = prm->W;
   const int R = H < kStripRows ? H : kStripRows;
   const int nstrips = (H + R - 1) / R;
-  // chunk = m strips; about 16 chunks unless the caller asks otherwise
+  // chunks of m strips (about 16 chunks unless the caller asks otherwise)
+  // after a ramp of 1, 1, 2, 4 strips; chunk c = strips cb[c] .. cb[c+1]-1
   int m = chunk_rows > 0 ? (chunk_rows + R - 1) / R : (nstrips + 15) / 16;
   if (m < 1) m = 1;
-  if ((nstrips + m - 1) / m > kMaxChunks) m = (nstrips + kMaxChunks - 1) / kMaxChunks;
-  const int K = (nstrips + m - 1) / m;
+  if ((nstrips + m - 1) / m > kMaxChunks - 4) m = (nstrips + kMaxChunks - 5) / (kMaxChunks - 4);
+  std::vector<int> cb{0};
+  for (int sz : {1, 1, 2, 4})
+    if (cb.back() < nstrips) cb.push_back(std::min(cb.back() + std::min(sz, m), nstrips));
+  while (cb.back() < nstrips) cb.push_back(std::min(cb.back() + m, nstrips));
+  const int K = (int)cb.size() - 1;
   auto rows_of = [&](int c, int& r0, int& r1) {
-    r0 = c * m * R;
-    r1 = (c + 1) * m * R < H ? (c + 1) * m * R : H;
+    r0 = cb[c] * R;
+    r1 = std::min(cb[c + 1] * R, H);
   };
   // compute order: chunks whose neighbours do not wrap first
   std::vector<int> order;
@@ -180,7 +189,7 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
         if (cudaStreamWaitEvent(s, pipe.ev_up[need], 0) != cudaSuccess)
           return check_launch("fd_fused_step_packed_host: wait for upload");
       }
-      const int s0 = c * m, ns = (c + 1) * m < nstrips ? m : nstrips - c * m;
+      const int s0 = cb[c], ns = cb[c + 1] - cb[c];
       if (int r = fused_tma_strips(*prm, *st, coef, mask, inlet_ux, src, dst, sin, sout, R, s0, ns, seed, s))
         return r;
       if (last) {

@@ -275,8 +275,9 @@ int fd_fused_step_packed_noalloc(const fd_params* prm, const fd_storage* st, con
  * fd_fused_step_packed); the device state after the call is in pop_b / side_b
  * when nsteps is odd, else in pop_a / side_a.  The upload, the first and last
  * iterations and the download are pipelined over chunks of about chunk_rows
- * rows (<= 0: about 16 chunks; rounded to whole strips of 16 rows): both copy
- * directions run at once and the kernels run under them.  host_in may equal
+ * rows (<= 0: about 1/16 of the lattice; rounded to whole strips of 16 rows,
+ * after four smaller leading chunks): both copy directions run at once and
+ * the kernels run under them.  host_in may equal
  * host_out.  Host buffers should be pinned (cudaHostAlloc / cudaHostRegister),
  * or the copies do not overlap.  W must be a multiple of 8.  Asynchronous on
  * `stream` like every step; uses two internal streams per device, and calls on

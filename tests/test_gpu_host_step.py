@@ -46,7 +46,7 @@ def pinned_copy(t):
 
 
 CASES = [("walls", 75, 96, "f32"), ("periodic", 130, 256, "f32"), ("walls", 130, 256, "f16"),
-         ("periodic", 74, 96, "bf16"), ("walls", 75, 96, "bf16")]
+         ("periodic", 74, 96, "bf16"), ("walls", 75, 96, "bf16"), ("walls", 1000, 64, "f32")]
 
 
 @pytest.mark.parametrize("variant,H,W,dtype", CASES, ids=[f"{c[0]}_{c[1]}x{c[2]}_{c[3]}" for c in CASES])
