@@ -64,13 +64,15 @@ template <typename SF, int NT, bool STOCH>
 int prepare(fd_batch* b) {
   using M = TmaSmem<SF, NT, tma_ring_depth<SF>()>;
   auto kern = k_fused_tma_batch<SF, NT, tma_ring_depth<SF>(), false, STOCH>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, M::BYTES) != cudaSuccess)
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, M::ALLOC) != cudaSuccess)
     return check_launch("fd_batch: shared-memory attribute");
   std::vector<BatchInst<SF>> hi(b->n);
   std::vector<int4> tiles;
   for (int i = 0; i < b->n; ++i) {
     hi[i].args[0] = instance_args<SF>(b->inst[i], b->st, b->rows, false);
     hi[i].args[1] = instance_args<SF>(b->inst[i], b->st, b->rows, true);
+    if (int r = tma_maps<SF, NT>(hi[i].args[0], (const char*)b->inst[i].pop_a, hi[i].maps[0])) return r;
+    if (int r = tma_maps<SF, NT>(hi[i].args[1], (const char*)b->inst[i].pop_b, hi[i].maps[1])) return r;
     const int nb = (b->inst[i].prm.W + NT - 1) / NT, ns = hi[i].args[0].nstrips;
     for (int s = 0; s < ns; ++s)
       for (int bb = 0; bb < nb; ++bb) tiles.push_back(make_int4(i, bb, s, 0));
@@ -96,7 +98,7 @@ int prepare(fd_batch* b) {
     return check_launch("fd_batch: table upload");
   b->ntiles = (int)tiles.size();
   int per_sm = 1, dev = 0, sms = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, M::BYTES);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, M::ALLOC);
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   b->grid = per_sm * sms;
@@ -108,7 +110,7 @@ int prepare(fd_batch* b) {
 template <typename SF, int NT, bool STOCH>
 void launch_one(const fd_batch* b, int parity, cudaStream_t st) {
   using M = TmaSmem<SF, NT, tma_ring_depth<SF>()>;
-  k_fused_tma_batch<SF, NT, tma_ring_depth<SF>(), false, STOCH><<<b->grid, NT, M::BYTES, st>>>(
+  k_fused_tma_batch<SF, NT, tma_ring_depth<SF>(), false, STOCH><<<b->grid, NT, M::ALLOC, st>>>(
       (const BatchInst<SF>*)b->d_inst, b->d_tiles, b->ntiles, parity, b->d_ctl);
 }
 

@@ -44,7 +44,9 @@ int tma_strips_t(const fd_params& p, const DevCoef& c, const uint16_t* mask, con
   constexpr int NS = tma_ring_depth<SF>();
   DevArgs<SF> a = tma_args<SF, FD_TMA_NT, NS, SCALED, STOCH>(p, c, mask, inlet_ux, R);
   tma_set_step(a, (const char*)src, (char*)dst, (float*)side_in, (float*)side_out, seed);
-  return launch_tma_strips<SF, FD_TMA_NT, NS, SCALED, STOCH>(a, strip0, nstrips, s);
+  TmaMaps tm;
+  if (int r = tma_maps<SF, FD_TMA_NT>(a, (const char*)src, tm)) return r;
+  return launch_tma_strips<SF, FD_TMA_NT, NS, SCALED, STOCH>(a, tm, strip0, nstrips, s);
 }
 
 template <typename SF>

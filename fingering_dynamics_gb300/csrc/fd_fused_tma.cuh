@@ -30,6 +30,7 @@
 
 #include "fd_fused_dev.cuh"
 #include "fd_host.h"
+#include "fd_tmap.h"
 
 // Band width (threads per CTA) of the single-lattice launch, and ring depth
 // per storage type for both launches (NS == 4: the split ring; NS >= 5:
@@ -83,6 +84,16 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
+// One box of a 3-D tensor map (coordinates x, row, plane) into shared memory
+// (128-byte aligned destination; x * element size a multiple of 16 bytes).
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
@@ -107,7 +118,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsign
   return false;
 }
 
-// Byte layout of one ring slot for a band of NT cells.
+// Byte layout of one ring slot for a band of NT cells: the nine f plane rows,
+// the eight g_i plane rows (from a 128-byte boundary: both blocks are
+// tensor-map boxes), the FP32 g_0 row and the mask row.  TENSOR: a band row
+// of an SF plane fits one box (at most 256 cells); wider bands copy each
+// plane row with a 1-D bulk copy.
 template <typename SF, int NT>
 struct SlotLayout {
   static constexpr int HF = 16 / (int)sizeof(SF);     // halo elements of an SF plane
@@ -116,10 +131,14 @@ struct SlotLayout {
   static constexpr int RF = ((NT + 2 * HF) * (int)sizeof(SF) + 15) / 16 * 16;
   static constexpr int RG = ((NT + 2 * HG) * 4 + 15) / 16 * 16;
   static constexpr int RM = ((NT + 2 * HM) * 2 + 15) / 16 * 16;
-  static constexpr int OFF_G0 = 9 * RF;
-  static constexpr int OFF_GI = OFF_G0 + RG;
-  static constexpr int OFF_M = OFF_GI + 8 * RF;
+  static constexpr bool TENSOR = NT + 2 * HF <= 256;
+  static_assert(RF == (NT + 2 * HF) * (int)sizeof(SF), "a plane row is one dense box row");
+  static constexpr int OFF_GI = (9 * RF + 127) / 128 * 128;
+  static constexpr int OFF_G0 = OFF_GI + 8 * RF;
+  static constexpr int OFF_M = OFF_G0 + RG;
   static constexpr int BYTES = (OFF_M + RM + 127) / 128 * 128;
+  // tensor-map boxes land on 128-byte boundaries, bulk copies on 16-byte ones
+  static_assert(OFF_GI % 128 == 0 && OFF_G0 % 16 == 0 && OFF_M % 16 == 0 && RM % 16 == 0, "slot alignment");
 };
 
 // Shared memory of the staged kernel.  NS >= 5: a ring of NS whole-row slots
@@ -140,8 +159,15 @@ struct TmaSmem {
   static constexpr int OFF_SLOT = (OFF_MASK + MASK_ROWS * L::RM + 127) / 128 * 128;
   static constexpr int SLOT = SPLIT ? (L::OFF_M + 127) / 128 * 128 : L::BYTES;
   static constexpr int BYTES = OFF_SLOT + NS * SLOT;
+  static constexpr int ALLOC = BYTES + 128;  // dynamic shared memory: BYTES from a 128-byte boundary
   static_assert(NBAR * 8 <= OFF_PSI, "mbarriers overlap the psi ring");
+  static_assert(OFF_SLOT % 128 == 0 && SLOT % 128 == 0 && OFF_MASK % 16 == 0, "slots on 128-byte boundaries");
 };
+
+// The 128-byte aligned start of the dynamic shared memory.
+__device__ __forceinline__ char* smem_aligned(char* raw) {
+  return raw + ((128u - (smem_u32(raw) & 127u)) & 127u);
+}
 
 // The part of lattice row r (wrapped into [0, H)) that a band loads: per kind
 // of plane the first loaded cell, the bytes per plane row and the byte offset
@@ -150,12 +176,14 @@ struct TmaSmem {
 template <typename SF, int NT>
 struct RowSpan {
   size_t rowoff;
+  int y;  // the row, wrapped into [0, H)
   int xs, gs, ms;
   unsigned nf, ng, nm;
   int df, dg, dm;
   __device__ __forceinline__ RowSpan(int r, int x0, int H, int W) {
     using L = SlotLayout<SF, NT>;
-    rowoff = (size_t)wrap(r, H) * W;
+    y = wrap(r, H);
+    rowoff = (size_t)y * W;
     xs = max(x0 - L::HF, 0);
     gs = max(x0 - L::HG, 0);
     ms = max(x0 - L::HM, 0);
@@ -168,48 +196,72 @@ struct RowSpan {
   }
 };
 
+// Bytes one SF plane row of the band brings into its slot: a whole box row
+// (cells beyond the lattice's x edges read as zero) or the clipped span.
 template <typename SF, int NT>
-__device__ __forceinline__ void copy_f_half(const DevArgs<SF>& a, char* slot, uint64_t* bar, const RowSpan<SF, NT>& s) {
-  using L = SlotLayout<SF, NT>;
-#pragma unroll
-  for (int i = 0; i < 9; ++i) bulk_g2s(slot + i * L::RF + s.df, a.src_f + i * a.pstride_f + s.rowoff + s.xs, s.nf, bar);
+__device__ __forceinline__ unsigned plane_row_bytes(const RowSpan<SF, NT>& s) {
+  if constexpr (SlotLayout<SF, NT>::TENSOR) return (unsigned)SlotLayout<SF, NT>::RF;
+  else return s.nf;
 }
 
+// The nine f plane rows: one tensor-map box, or a bulk copy per plane.
 template <typename SF, int NT>
-__device__ __forceinline__ void copy_g_half(const DevArgs<SF>& a, char* slot, uint64_t* bar, const RowSpan<SF, NT>& s) {
+__device__ __forceinline__ void copy_f_half(const DevArgs<SF>& a, const TmaMaps* tm, char* slot, uint64_t* bar,
+                                            const RowSpan<SF, NT>& s, int x0) {
+  using L = SlotLayout<SF, NT>;
+  if constexpr (L::TENSOR) {
+    tma_load_3d(slot, &tm->f, x0 - L::HF, s.y, 0, bar);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+      bulk_g2s(slot + i * L::RF + s.df, a.src_f + i * a.pstride_f + s.rowoff + s.xs, s.nf, bar);
+  }
+}
+
+// The eight g_i plane rows (one box, or a bulk copy per plane) and the FP32
+// g_0 row (a bulk copy).
+template <typename SF, int NT>
+__device__ __forceinline__ void copy_g_half(const DevArgs<SF>& a, const TmaMaps* tm, char* slot, uint64_t* bar,
+                                            const RowSpan<SF, NT>& s, int x0) {
   using L = SlotLayout<SF, NT>;
   bulk_g2s(slot + L::OFF_G0 + s.dg, a.src_g0 + s.rowoff + s.gs, s.ng, bar);
+  if constexpr (L::TENSOR) {
+    tma_load_3d(slot + L::OFF_GI, &tm->gi, x0 - L::HF, s.y, 0, bar);
+  } else {
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
-    bulk_g2s(slot + L::OFF_GI + i * L::RF + s.df, a.src_gi + i * a.pstride_f + s.rowoff + s.xs, s.nf, bar);
+    for (int i = 0; i < 8; ++i)
+      bulk_g2s(slot + L::OFF_GI + i * L::RF + s.df, a.src_gi + i * a.pstride_f + s.rowoff + s.xs, s.nf, bar);
+  }
 }
 
-// Issue the bulk copies of lattice row r into a whole-row slot (NS >= 5).
+// Issue the copies of lattice row r into a whole-row slot (NS >= 5).
 template <typename SF, int NT>
-__device__ __forceinline__ void issue_row(const DevArgs<SF>& a, char* slot, uint64_t* bar, int r, int x0) {
+__device__ __forceinline__ void issue_row(const DevArgs<SF>& a, const TmaMaps* tm, char* slot, uint64_t* bar, int r,
+                                          int x0) {
   using L = SlotLayout<SF, NT>;
   const RowSpan<SF, NT> s(r, x0, a.H, a.W);
-  mbar_expect_tx(bar, 17 * s.nf + s.ng + s.nm);
-  copy_f_half<SF, NT>(a, slot, bar, s);
-  copy_g_half<SF, NT>(a, slot, bar, s);
+  mbar_expect_tx(bar, 17 * plane_row_bytes(s) + s.ng + s.nm);
+  copy_f_half<SF, NT>(a, tm, slot, bar, s, x0);
+  copy_g_half<SF, NT>(a, tm, slot, bar, s, x0);
   bulk_g2s(slot + L::OFF_M + s.dm, a.mask + s.rowoff + s.ms, s.nm, bar);
 }
 
 // Split ring (NS == 4): the g half of row r with its mask row, and the f half.
 template <typename SF, int NT>
-__device__ __forceinline__ void issue_g_half(const DevArgs<SF>& a, char* slot, char* mrow, uint64_t* bar, int r,
-                                             int x0) {
+__device__ __forceinline__ void issue_g_half(const DevArgs<SF>& a, const TmaMaps* tm, char* slot, char* mrow,
+                                             uint64_t* bar, int r, int x0) {
   const RowSpan<SF, NT> s(r, x0, a.H, a.W);
-  mbar_expect_tx(bar, 8 * s.nf + s.ng + s.nm);
-  copy_g_half<SF, NT>(a, slot, bar, s);
+  mbar_expect_tx(bar, 8 * plane_row_bytes(s) + s.ng + s.nm);
+  copy_g_half<SF, NT>(a, tm, slot, bar, s, x0);
   bulk_g2s(mrow + s.dm, a.mask + s.rowoff + s.ms, s.nm, bar);
 }
 
 template <typename SF, int NT>
-__device__ __forceinline__ void issue_f_half(const DevArgs<SF>& a, char* slot, uint64_t* bar, int r, int x0) {
+__device__ __forceinline__ void issue_f_half(const DevArgs<SF>& a, const TmaMaps* tm, char* slot, uint64_t* bar,
+                                             int r, int x0) {
   const RowSpan<SF, NT> s(r, x0, a.H, a.W);
-  mbar_expect_tx(bar, 9 * s.nf);
-  copy_f_half<SF, NT>(a, slot, bar, s);
+  mbar_expect_tx(bar, 9 * plane_row_bytes(s));
+  copy_f_half<SF, NT>(a, tm, slot, bar, s, x0);
 }
 
 // Shared-memory load of element idx of a plane row at byte offset `off` from
@@ -277,8 +329,8 @@ __device__ __forceinline__ float psi_cell(const char* sm, const DevArgs<SF>& a, 
 // (per-slot parity of the next fill to wait for) and `ok` carry over from
 // strip to strip.  Ends with a CTA barrier, so the ring can be refilled.
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
-__device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, int band, int strip, char* smem, unsigned& phase,
-                                               bool& ok) {
+__device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMaps* tm, int band, int strip, char* smem,
+                                               unsigned& phase, bool& ok) {
   static_assert(NS >= 5, "rows y-2 .. y+2 must be resident while row y is computed");
   using L = SlotLayout<SF, NT>;
   using M = TmaSmem<SF, NT, NS>;
@@ -300,7 +352,7 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, int band, i
   // row first + k lives in slot k (mod NS); rows y0-2 .. y0+NS-3 fill slots 0..NS-1
   if (t == 0) {
     for (int k = 0; k < NS && first + k <= last; ++k)
-      issue_row<SF, NT>(a, smem + M::OFF_SLOT + k * M::SLOT, &bars[k], first + k, x0);
+      issue_row<SF, NT>(a, tm, smem + M::OFF_SLOT + k * M::SLOT, &bars[k], first + k, x0);
   }
   auto wait_slot = [&](int s) {
     if (ok) ok = mbar_wait(&bars[s], (phase >> s) & 1u);
@@ -371,7 +423,7 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, int band, i
     }
     // 2. psi(y+1) complete; the slot of row y-2 is free for row y+NS-2
     __syncthreads();
-    if (t == 0 && y + NS - 2 <= last) issue_row<SF, NT>(a, smem + so[0], &bars[si[0]], y + NS - 2, x0);
+    if (t == 0 && y + NS - 2 <= last) issue_row<SF, NT>(a, tm, smem + so[0], &bars[si[0]], y + NS - 2, x0);
     // 3. stencils, f pull, Zou-He, collision, store
     if (owned) {
       const float* pm = psi_row(0);
@@ -484,8 +536,8 @@ __device__ __forceinline__ float inlet_corner_drho(const DevArgs<SF>& a, int yn)
 // row y0-2 is never needed (the inlet corners read global memory), so the
 // prologue fills f rows y0-1 .. y0+2.
 template <typename SF, int NT, bool SCALED, bool STOCH>
-__device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, int band, int strip, char* smem,
-                                                unsigned& phase, bool& ok) {
+__device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaMaps* tm, int band, int strip,
+                                                char* smem, unsigned& phase, bool& ok) {
   using L = SlotLayout<SF, NT>;
   using M = TmaSmem<SF, NT, 4>;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
@@ -508,13 +560,13 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, int band, 
   auto issue_g = [&](int r) {
     if (r > last || !ok) return;
     const int b = (r - first) & 3;
-    issue_g_half<SF, NT>(a, smem + slot(r), smem + mrow(r), &bars[b], r, x0);
+    issue_g_half<SF, NT>(a, tm, smem + slot(r), smem + mrow(r), &bars[b], r, x0);
     issued ^= 1u << b;
   };
   auto issue_f = [&](int r) {
     if (r > y1 || !ok) return;
     const int b = 4 + ((r - first) & 3);
-    issue_f_half<SF, NT>(a, smem + slot(r), &bars[b], r, x0);
+    issue_f_half<SF, NT>(a, tm, smem + slot(r), &bars[b], r, x0);
     issued ^= 1u << b;
   };
   auto wait_bar = [&](int b) {
@@ -645,10 +697,10 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, int band, 
 }
 
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
-__device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, int band, int strip, char* smem, unsigned& phase,
-                                          bool& ok) {
-  if constexpr (NS == 4) tma_strip_split<SF, NT, SCALED, STOCH>(a, band, strip, smem, phase, ok);
-  else tma_strip_ring<SF, NT, NS, SCALED, STOCH>(a, band, strip, smem, phase, ok);
+__device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, const TmaMaps* tm, int band, int strip, char* smem,
+                                          unsigned& phase, bool& ok) {
+  if constexpr (NS == 4) tma_strip_split<SF, NT, SCALED, STOCH>(a, tm, band, strip, smem, phase, ok);
+  else tma_strip_ring<SF, NT, NS, SCALED, STOCH>(a, tm, band, strip, smem, phase, ok);
 }
 
 template <typename SF, int NT, int NS>
@@ -662,21 +714,27 @@ __device__ __forceinline__ void init_ring(char* smem) {
   __syncthreads();
 }
 
-// CTA b takes band b % nbands of strip strip0 + b / nbands.
+// CTA b takes band b % nbands of strip strip0 + b / nbands.  `tm`: the tensor
+// maps of the step's source planes (a grid constant: TMA reads it from the
+// parameter space).
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
-__global__ void __launch_bounds__(NT) k_fused_tma(const DevArgs<SF> a, int nbands, int strip0) {
-  extern __shared__ __align__(128) char smem[];
+__global__ void __launch_bounds__(NT) k_fused_tma(const __grid_constant__ DevArgs<SF> a, int nbands, int strip0,
+                                                  const __grid_constant__ TmaMaps tm) {
+  extern __shared__ __align__(128) char smem_raw[];
+  char* smem = smem_aligned(smem_raw);
   init_ring<SF, NT, NS>(smem);
   unsigned phase = 0;
   bool ok = true;
-  tma_strip<SF, NT, NS, SCALED, STOCH>(a, (int)blockIdx.x % nbands, strip0 + (int)blockIdx.x / nbands, smem, phase,
-                                       ok);
+  tma_strip<SF, NT, NS, SCALED, STOCH>(a, &tm, (int)blockIdx.x % nbands, strip0 + (int)blockIdx.x / nbands, smem,
+                                       phase, ok);
 }
 
-// One lattice of a batch: its arguments for both ping-pong parities.
+// One lattice of a batch: its arguments and the tensor maps of its source
+// planes for both ping-pong parities (in global memory, where TMA reads them).
 template <typename SF>
 struct BatchInst {
   DevArgs<SF> args[2];
+  TmaMaps maps[2];
 };
 
 // Persistent kernel over a tile table of (instance, band, strip) entries,
@@ -696,9 +754,11 @@ template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 __global__ void __launch_bounds__(NT) k_fused_tma_batch(const BatchInst<SF>* __restrict__ inst,
                                                         const int4* __restrict__ tiles, int ntiles, int parity,
                                                         unsigned* __restrict__ ctl) {
-  extern __shared__ __align__(128) char smem[];
+  extern __shared__ __align__(128) char smem_raw[];
   __shared__ DevArgs<SF> sa;
+  __shared__ const TmaMaps* stm;
   __shared__ int next;
+  char* smem = smem_aligned(smem_raw);
   init_ring<SF, NT, NS>(smem);
   unsigned done = 0;
   if constexpr (STOCH) done = ctl[parity];
@@ -713,6 +773,7 @@ __global__ void __launch_bounds__(NT) k_fused_tma_batch(const BatchInst<SF>* __r
       next = (int)atomicAdd(&ctl[2 + parity], 1u);
       if (next < ntiles) {
         sa = inst[tiles[next].x].args[parity];
+        stm = &inst[tiles[next].x].maps[parity];
         if constexpr (STOCH) sa.seed = sr_hash(sa.seed + done);
       }
     }
@@ -720,7 +781,7 @@ __global__ void __launch_bounds__(NT) k_fused_tma_batch(const BatchInst<SF>* __r
     const int k = next;
     if (k >= ntiles || !ok) break;
     const int4 tl = tiles[k];
-    tma_strip<SF, NT, NS, SCALED, STOCH>(sa, tl.y, tl.z, smem, phase, ok);
+    tma_strip<SF, NT, NS, SCALED, STOCH>(sa, stm, tl.y, tl.z, smem, phase, ok);
   }
 }
 
@@ -732,7 +793,21 @@ namespace fd {
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 cudaError_t tma_prepare_kernel() {
   static std::atomic<unsigned long long> attr_done{0};
-  return ensure_smem_attr(k_fused_tma<SF, NT, NS, SCALED, STOCH>, TmaSmem<SF, NT, NS>::BYTES, attr_done);
+  return ensure_smem_attr(k_fused_tma<SF, NT, NS, SCALED, STOCH>, TmaSmem<SF, NT, NS>::ALLOC, attr_done);
+}
+
+// Tensor maps of the f and g_i planes of the packed buffer `src` (bands of NT
+// cells; unused, and left empty, when a band row does not fit one box).
+template <typename SF, int NT>
+int tma_maps(const DevArgs<SF>& a, const char* src, TmaMaps& m) {
+  using L = SlotLayout<SF, NT>;
+  m = TmaMaps{};
+  if constexpr (!L::TENSOR) return FD_OK;
+  const PackedLayout<SF> P = packed_layout<SF>(a.H, a.W);
+  const int es = (int)sizeof(SF), box = NT + 2 * L::HF;
+  const size_t pb = P.pstride * sizeof(SF);
+  if (int r = encode_plane_rows(&m.f, src + P.off_f, es, a.W, a.H, 9, pb, box)) return r;
+  return encode_plane_rows(&m.gi, src + P.off_gi, es, a.W, a.H, 8, pb, box);
 }
 
 // Arguments of the staged kernel for one lattice with strips of R rows; the
@@ -759,7 +834,7 @@ DevArgs<SF> tma_args(const fd_params& p, const DevCoef& c, const uint16_t* mask,
   if (R <= 0) {
     int per_sm = 1;
     tma_prepare_kernel<SF, NT, NS, SCALED, STOCH>();  // the occupancy depends on the raised limit
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tma<SF, NT, NS, SCALED, STOCH>, NT, M::BYTES);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tma<SF, NT, NS, SCALED, STOCH>, NT, M::ALLOC);
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -792,14 +867,15 @@ void tma_set_step(DevArgs<SF>& a, const char* src, char* dst, float* side_in, fl
   a.seed = sr_hash(seed);
 }
 
-// One step over strips strip0 .. strip0 + nstrips - 1 of the lattice.
+// One step over strips strip0 .. strip0 + nstrips - 1 of the lattice; `tm`:
+// the tensor maps of the step's source buffer (tma_maps).
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
-int launch_tma_strips(const DevArgs<SF>& a, int strip0, int nstrips, cudaStream_t st) {
+int launch_tma_strips(const DevArgs<SF>& a, const TmaMaps& tm, int strip0, int nstrips, cudaStream_t st) {
   using M = TmaSmem<SF, NT, NS>;
   if (tma_prepare_kernel<SF, NT, NS, SCALED, STOCH>() != cudaSuccess) return FD_ERR_CUDA;
   if (nstrips <= 0) return FD_OK;
   const unsigned blocks = (unsigned)(a.nchunks * nstrips);
-  k_fused_tma<SF, NT, NS, SCALED, STOCH><<<blocks, NT, M::BYTES, st>>>(a, a.nchunks, strip0);
+  k_fused_tma<SF, NT, NS, SCALED, STOCH><<<blocks, NT, M::ALLOC, st>>>(a, a.nchunks, strip0, tm);
   return FD_OK;
 }
 
@@ -807,10 +883,13 @@ template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 int launch_fused_tma(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, char* pa,
                      char* pb, float* sa, float* sb, int nsteps, int R, uint32_t seed, cudaStream_t st) {
   DevArgs<SF> a = tma_args<SF, NT, NS, SCALED, STOCH>(p, c, mask, inlet_ux, R);
+  TmaMaps from_a, from_b;  // the source planes of even and of odd steps
+  if (int r = tma_maps<SF, NT>(a, pa, from_a)) return r;
+  if (int r = tma_maps<SF, NT>(a, pb, from_b)) return r;
   for (int s = 0; s < nsteps; ++s) {
     const bool even = s % 2 == 0;
     tma_set_step(a, even ? pa : pb, even ? pb : pa, even ? sa : sb, even ? sb : sa, seed + (uint32_t)s);
-    if (int r = launch_tma_strips<SF, NT, NS, SCALED, STOCH>(a, 0, a.nstrips, st)) return r;
+    if (int r = launch_tma_strips<SF, NT, NS, SCALED, STOCH>(a, even ? from_a : from_b, 0, a.nstrips, st)) return r;
   }
   return cudaGetLastError() == cudaSuccess ? FD_OK : FD_ERR_CUDA;
 }

@@ -42,7 +42,7 @@ struct Pipe {
   std::mutex mu;
   bool ready = false;
   cudaStream_t up = nullptr, down = nullptr;
-  cudaEvent_t fork = nullptr, done_down = nullptr;
+  cudaEvent_t fork = nullptr, up_done = nullptr, done_down = nullptr;
   std::vector<cudaEvent_t> ev_up, ev_comp;
 };
 
@@ -53,7 +53,7 @@ int pipe_init(Pipe& p) {
   auto ev = [](cudaEvent_t* e) { return cudaEventCreateWithFlags(e, cudaEventDisableTiming); };
   if (cudaStreamCreateWithFlags(&p.up, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&p.down, cudaStreamNonBlocking) != cudaSuccess || ev(&p.fork) != cudaSuccess ||
-      ev(&p.done_down) != cudaSuccess)
+      ev(&p.up_done) != cudaSuccess || ev(&p.done_down) != cudaSuccess)
     return check_launch("fd_fused_step_packed_host: stream/event creation");
   p.ev_up.resize(kMaxChunks);
   p.ev_comp.resize(kMaxChunks);
@@ -96,6 +96,12 @@ cudaError_t copy_rows(const Planes& q, int W, int r0, int r1, char* dst, const c
   return e;
 }
 
+// Enqueue the uploads, the iterations and the downloads (after the fork).
+int host_pipeline(Pipe& pipe, const fd_params& prm, const fd_storage& st, const DevCoef& coef, const uint16_t* mask,
+                  const double* inlet_ux, const Planes& q, const std::vector<int>& cb, const std::vector<int>& order,
+                  int R, int nstrips, int nsteps, const char* hin, char* hout, char* pa, char* pb, float* sa,
+                  float* sb, cudaStream_t s);
+
 }  // namespace
 }  // namespace fd
 
@@ -122,7 +128,7 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
   if (cudaGetDevice(&dev) != cudaSuccess) return check_launch("fd_fused_step_packed_host");
   FD_REQUIRE(dev >= 0 && dev < 64, FD_ERR_ARG, "fd_fused_step_packed_host: device ordinal %d", dev);
 
-  const int H = prm->H, W = prm->W;
+  const int H = prm->H;
   const int R = H < kStripRows ? H : kStripRows;
   const int nstrips = (H + R - 1) / R;
   // chunks of m strips (about 16 chunks unless the caller asks otherwise)
@@ -135,10 +141,6 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
     if (cb.back() < nstrips) cb.push_back(std::min(cb.back() + std::min(sz, m), nstrips));
   while (cb.back() < nstrips) cb.push_back(std::min(cb.back() + m, nstrips));
   const int K = (int)cb.size() - 1;
-  auto rows_of = [&](int c, int& r0, int& r1) {
-    r0 = cb[c] * R;
-    r1 = std::min(cb[c + 1] * R, H);
-  };
   // compute order: chunks whose neighbours do not wrap first
   std::vector<int> order;
   for (int c = 1; c + 1 < K; ++c) order.push_back(c);
@@ -163,6 +165,31 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
   if (cudaEventRecord(pipe.fork, s) != cudaSuccess || cudaStreamWaitEvent(pipe.up, pipe.fork, 0) != cudaSuccess ||
       cudaStreamWaitEvent(pipe.down, pipe.fork, 0) != cudaSuccess)
     return check_launch("fd_fused_step_packed_host: fork");
+  const int r = host_pipeline(pipe, *prm, *st, coef, mask, inlet_ux, q, cb, order, R, nstrips, nsteps, hin, hout, pa,
+                              pb, sa, sb, s);
+  // join, also after a failure: the caller's stream continues after the
+  // copies already issued on both internal streams
+  const bool joined = cudaEventRecord(pipe.up_done, pipe.up) == cudaSuccess &&
+                      cudaEventRecord(pipe.done_down, pipe.down) == cudaSuccess &&
+                      cudaStreamWaitEvent(s, pipe.up_done, 0) == cudaSuccess &&
+                      cudaStreamWaitEvent(s, pipe.done_down, 0) == cudaSuccess;
+  if (r != FD_OK) return r;
+  if (!joined) return check_launch("fd_fused_step_packed_host: join");
+  return check_launch("fd_fused_step_packed_host");
+}
+
+namespace fd {
+namespace {
+
+int host_pipeline(Pipe& pipe, const fd_params& prm, const fd_storage& st, const DevCoef& coef, const uint16_t* mask,
+                  const double* inlet_ux, const Planes& q, const std::vector<int>& cb, const std::vector<int>& order,
+                  int R, int nstrips, int nsteps, const char* hin, char* hout, char* pa, char* pb, float* sa,
+                  float* sb, cudaStream_t s) {
+  const int K = (int)cb.size() - 1, H = prm.H, W = prm.W;
+  auto rows_of = [&](int c, int& r0, int& r1) {
+    r0 = cb[c] * R;
+    r1 = std::min(cb[c + 1] * R, H);
+  };
   for (int c = 0; c < K; ++c) {
     int r0, r1;
     rows_of(c, r0, r1);
@@ -176,10 +203,10 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
     char* dst = even ? pb : pa;
     float* sin = even ? sa : sb;
     float* sout = even ? sb : sa;
-    const uint32_t seed = st->seed + (uint32_t)step;
+    const uint32_t seed = st.seed + (uint32_t)step;
     const bool first = step == 0, last = step == nsteps - 1;
     if (!first && !last) {  // a middle step: one launch over the whole lattice
-      if (int r = fused_tma_strips(*prm, *st, coef, mask, inlet_ux, src, dst, sin, sout, R, 0, nstrips, seed, s))
+      if (int r = fused_tma_strips(prm, st, coef, mask, inlet_ux, src, dst, sin, sout, R, 0, nstrips, seed, s))
         return r;
       continue;
     }
@@ -190,7 +217,7 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
           return check_launch("fd_fused_step_packed_host: wait for upload");
       }
       const int s0 = cb[c], ns = cb[c + 1] - cb[c];
-      if (int r = fused_tma_strips(*prm, *st, coef, mask, inlet_ux, src, dst, sin, sout, R, s0, ns, seed, s))
+      if (int r = fused_tma_strips(prm, st, coef, mask, inlet_ux, src, dst, sin, sout, R, s0, ns, seed, s))
         return r;
       if (last) {
         int r0, r1;
@@ -202,9 +229,8 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
       }
     }
   }
-  // join: the caller's stream continues after the last download
-  if (cudaEventRecord(pipe.done_down, pipe.down) != cudaSuccess ||
-      cudaStreamWaitEvent(s, pipe.done_down, 0) != cudaSuccess)
-    return check_launch("fd_fused_step_packed_host: join");
-  return check_launch("fd_fused_step_packed_host");
+  return FD_OK;
 }
+
+}  // namespace
+}  // namespace fd

@@ -361,7 +361,8 @@ def generate_trajectories(specs, n_frames: int, jump: int = 200, dtype: str = "f
         torch.cuda.current_stream().wait_stream(ens.stream)
         for m, lat in enumerate(ens.lattices):
             frames[m, k] = member_frame(lat)[..., :4]
-    finite = torch.isfinite(frames.float().view(len(specs), -1)).all(dim=1)
+    # per member, in the storage type (an FP32 copy of every frame would double the footprint)
+    finite = torch.stack([torch.isfinite(frames[m]).all() for m in range(len(specs))])
     ens.close()
     return frames, finite
 
@@ -493,25 +494,36 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
     Plain: one batched ensemble of the members.  Accelerated, per round: one
     batched forward per jump for all members, every lattice restarted from
     the equilibrium of its predicted fields, `jump` batched LBM iterations as
-    the judge; a member whose judged saturation misses the surrogate's own
-    prediction for that iteration by more than `tol` (relative) is put back to
-    its state at the round's start (exactly) and advanced by plain batched
-    LBM instead.  Returns wall times, final saturations and acceptance."""
+    the judge (one batch over all members, built once: its CUDA graph is
+    captured once); a member whose judged saturation misses the surrogate's
+    own prediction for that iteration by more than `tol` (relative) is put
+    back to its state at the round's start (exactly) and advanced by plain
+    batched LBM instead.  Returns wall times, final saturations and
+    acceptance."""
     from .ensemble import Ensemble
     from .lattice import Lattice
 
     span = (jumps_per_check + 1) * jump
     horizon = rounds * span
 
-    def advance(lats, n):  # n iterations of every lattice (reference mode in and out) in one batch
-        ens = Ensemble.from_lattices(lats)
+    def advance(lats, n, ens=None):
+        """n iterations of every lattice (reference mode in and out) in one
+        batch: `ens` (a batch over exactly these lattices) or a new one."""
+        own = ens is None
+        if own:
+            ens = Ensemble.from_lattices(lats)
+        for lat in lats:
+            lat.enter_fused()
         ens.step(n - 1)
-        ens.close()
+        if own:
+            ens.close()
         for lat in lats:
             lat.exit_fused()
 
-    def sat(lat):
-        return saturation(lat.psi, lat.fluid)
+    def sats(lats):  # saturations of all lattices, one host synchronisation
+        v = torch.stack([((lat.psi > 0) & lat.fluid).sum().double() / lat.fluid.sum().clamp(min=1).double()
+                         for lat in lats])
+        return v.tolist()
 
     plain = [Lattice(p, g, dtype=dtype) for p, g in members]
     torch.cuda.synchronize()
@@ -519,7 +531,7 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
     advance(plain, horizon)
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t0
-    sat_plain = [sat(lat) for lat in plain]
+    sat_plain = sats(plain)
     del plain
     torch.cuda.empty_cache()
 
@@ -527,6 +539,7 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
     accepted = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    judge = None  # the batch over all members, built at the first judge
     for _ in range(rounds):
         ck = [lat.checkpoint() for lat in lats]
         x = torch.stack([frame_from_fields(lat.psi, lat.ux, lat.uy, ~lat.fluid) for lat in lats]).contiguous()
@@ -539,10 +552,11 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
             psi, ux, uy = fields_from_frame(x[m])
             lat.restart_from_fields(torch.where(lat.fluid, psi, lat.params.psi_wall), ux, uy, rho=lat.rho,
                                     iteration=lat.iteration + jumps_per_check * jump)
-        advance(lats, jump)
+        if judge is None:
+            judge = Ensemble.from_lattices(lats)
+        advance(lats, jump, judge)
         rejected = []
-        for m, lat in enumerate(lats):
-            s_lbm = sat(lat)
+        for m, s_lbm in enumerate(sats(lats)):
             if np.isfinite(s_lbm) and abs(s_lbm - sat_sur[m]) <= tol * max(s_lbm, 1e-12):
                 accepted += 1
             else:
@@ -551,9 +565,11 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
             lats[m].restore(ck[m])
         if rejected:
             advance([lats[m] for m in rejected], span)
+    if judge is not None:
+        judge.close()
     torch.cuda.synchronize()
     t_acc = time.perf_counter() - t0
-    sat_acc = [sat(lat) for lat in lats]
+    sat_acc = sats(lats)
     rel = [abs(a - p) / max(p, 1e-12) for a, p in zip(sat_acc, sat_plain)]
     return {"members": len(members), "rounds": rounds, "horizon_iterations": horizon,
             "plain_s": t_plain, "accelerated_s": t_acc, "speedup": t_plain / t_acc,
