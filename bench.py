@@ -418,6 +418,39 @@ def run_precision(args):
     return 0
 
 
+def run_accelerated(args):
+    """The surrogate-accelerated ensemble against the plain batched LBM on the
+    held-out members of the surrogate workload (same generator and seeds; the
+    last 10% of --members), with a network trained and saved by
+    `--workload surrogate --save-net`."""
+    import torch
+    from fingering_dynamics_gb300 import build
+    from fingering_dynamics_gb300.ensemble import ensemble_specs
+    from fingering_dynamics_gb300.surrogate import UNet, accelerated_ensemble
+    build.build()
+    if not args.load_net:
+        raise SystemExit("--workload accelerated needs --load-net (a network saved by --workload surrogate --save-net)")
+    H, W, jump = 256, 512, 200
+    M = args.members
+    specs = ensemble_specs(M, seed=2024, sizes_w=(W,), sizes_h=(H,))
+    held = max(1, M // 10)
+    net = UNet((32, 64, 128, 256), params=dict(np.load(args.load_net)), conv=args.conv)
+    members = [specs[i].build() for i in range(M - held, M)][:args.batch]
+    # pick the convolution kernels for the batch shape before the timed runs
+    net.predict(torch.zeros((len(members), H, W, 16), dtype=torch.bfloat16, device="cuda"))
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        acc = accelerated_ensemble(net, members, rounds=5, jump=jump)
+    line = {"metric": "surrogate-accelerated ensemble speed-up over the plain batched LBM, same horizon",
+            "value": round(acc["speedup"], 3), "unit": "x", "higher_is_better": True, "n_gpus": 1, "steps": 5,
+            "warmup": 0, "dtype": "bf16 network, f32 lattices", "data": "synthetic (held-out geometries)",
+            "config": {"workload": f"accelerated_{len(members)}_members_{W}x{H}", "rounds": 5,
+                       "jumps_per_check": 5, "jump": jump, "tolerance": 0.02},
+            "accelerated_ensemble": acc, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_surrogate(args):
     """BASELINE configs[4]: the learned surrogate at 512 x 256.  Trajectories of
     a seeded ensemble (batched LBM, one frame every 200 iterations), the last
@@ -457,6 +490,8 @@ def run_surrogate(args):
     ms_step = e0.elapsed_time(e1) / args.train_steps
     flops_step = 3.0 * net.flops_forward(args.batch, H, W)
     tflops = flops_step / (ms_step / 1e3) / 1e12
+    if args.save_net:
+        np.savez(args.save_net, **net.state_dict())
     ev = evaluate(net, test_f)
     roll = rollout_saturation_error(net, test_f, start=0, jumps=5)
     # one jump of `batch` members: surrogate forward vs 200 batched LBM iterations
@@ -560,7 +595,7 @@ def main():
     ap.add_argument("--H", type=int, default=H_FULL, help="lattice rows (default: the 4096 x 2048 workload)")
     ap.add_argument("--W", type=int, default=W_FULL, help="lattice columns")
     ap.add_argument("--workload", default="single",
-                    choices=["single", "ensemble", "precision", "surrogate", "surrogate-convs"],
+                    choices=["single", "ensemble", "precision", "surrogate", "surrogate-convs", "accelerated"],
                     help="single 4096 x 2048 lattice (default), the batched ensemble, or the error study of "
                          "reduced-precision storage against the FP64 path (1024 x 256, --steps iterations)")
     ap.add_argument("--rounding", default="stochastic", choices=["stochastic", "nearest"],
@@ -573,6 +608,9 @@ def main():
     ap.add_argument("--batch", type=int, default=32, help="surrogate: training batch")
     ap.add_argument("--conv", default="auto", choices=["auto", "mma", "tcgen05"],
                     help="surrogate: forward / data-gradient convolution kernel (auto: the faster per shape)")
+    ap.add_argument("--save-net", default=None, help="surrogate: write the trained network's weights (.npz) here")
+    ap.add_argument("--load-net", default=None,
+                    help="accelerated: the trained network's weights (.npz, as written by --save-net)")
     ap.add_argument("--family", default="stable", choices=["stable", "spec"],
                     help="ensemble parameter family (spec: the configuration's literal ranges)")
     args = ap.parse_args()
@@ -588,6 +626,8 @@ def main():
         return run_surrogate(args)
     if args.workload == "surrogate-convs":
         return run_convs(args)
+    if args.workload == "accelerated":
+        return run_accelerated(args)
     return run_ours(args)
 
 

@@ -138,7 +138,8 @@ struct SlotLayout {
   static constexpr int OFF_M = OFF_G0 + RG;
   static constexpr int BYTES = (OFF_M + RM + 127) / 128 * 128;
   // tensor-map boxes land on 128-byte boundaries, bulk copies on 16-byte ones
-  static_assert(OFF_GI % 128 == 0 && OFF_G0 % 16 == 0 && OFF_M % 16 == 0 && RM % 16 == 0, "slot alignment");
+  static_assert(OFF_GI % 128 == 0 && OFF_G0 % 128 == 0 && OFF_M % 16 == 0 && RM % 16 == 0, "slot alignment");
+  static_assert(!TENSOR || NT + 2 * HG <= 256, "the g_0 row fits one box when the SF rows do");
 };
 
 // Shared memory of the staged kernel.  NS >= 5: a ring of NS whole-row slots
@@ -218,16 +219,24 @@ __device__ __forceinline__ void copy_f_half(const DevArgs<SF>& a, const TmaMaps*
   }
 }
 
-// The eight g_i plane rows (one box, or a bulk copy per plane) and the FP32
-// g_0 row (a bulk copy).
+// Bytes the FP32 g_0 row of the band brings into its slot.
+template <typename SF, int NT>
+__device__ __forceinline__ unsigned g0_row_bytes(const RowSpan<SF, NT>& s) {
+  if constexpr (SlotLayout<SF, NT>::TENSOR) return (unsigned)SlotLayout<SF, NT>::RG;
+  else return s.ng;
+}
+
+// The eight g_i plane rows and the FP32 g_0 row: one box each, or a bulk copy
+// per plane.
 template <typename SF, int NT>
 __device__ __forceinline__ void copy_g_half(const DevArgs<SF>& a, const TmaMaps* tm, char* slot, uint64_t* bar,
                                             const RowSpan<SF, NT>& s, int x0) {
   using L = SlotLayout<SF, NT>;
-  bulk_g2s(slot + L::OFF_G0 + s.dg, a.src_g0 + s.rowoff + s.gs, s.ng, bar);
   if constexpr (L::TENSOR) {
+    tma_load_3d(slot + L::OFF_G0, &tm->g0, x0 - L::HG, s.y, 0, bar);
     tma_load_3d(slot + L::OFF_GI, &tm->gi, x0 - L::HF, s.y, 0, bar);
   } else {
+    bulk_g2s(slot + L::OFF_G0 + s.dg, a.src_g0 + s.rowoff + s.gs, s.ng, bar);
 #pragma unroll
     for (int i = 0; i < 8; ++i)
       bulk_g2s(slot + L::OFF_GI + i * L::RF + s.df, a.src_gi + i * a.pstride_f + s.rowoff + s.xs, s.nf, bar);
@@ -240,7 +249,7 @@ __device__ __forceinline__ void issue_row(const DevArgs<SF>& a, const TmaMaps* t
                                           int x0) {
   using L = SlotLayout<SF, NT>;
   const RowSpan<SF, NT> s(r, x0, a.H, a.W);
-  mbar_expect_tx(bar, 17 * plane_row_bytes(s) + s.ng + s.nm);
+  mbar_expect_tx(bar, 17 * plane_row_bytes(s) + g0_row_bytes(s) + s.nm);
   copy_f_half<SF, NT>(a, tm, slot, bar, s, x0);
   copy_g_half<SF, NT>(a, tm, slot, bar, s, x0);
   bulk_g2s(slot + L::OFF_M + s.dm, a.mask + s.rowoff + s.ms, s.nm, bar);
@@ -251,7 +260,7 @@ template <typename SF, int NT>
 __device__ __forceinline__ void issue_g_half(const DevArgs<SF>& a, const TmaMaps* tm, char* slot, char* mrow,
                                              uint64_t* bar, int r, int x0) {
   const RowSpan<SF, NT> s(r, x0, a.H, a.W);
-  mbar_expect_tx(bar, 8 * plane_row_bytes(s) + s.ng + s.nm);
+  mbar_expect_tx(bar, 8 * plane_row_bytes(s) + g0_row_bytes(s) + s.nm);
   copy_g_half<SF, NT>(a, tm, slot, bar, s, x0);
   bulk_g2s(mrow + s.dm, a.mask + s.rowoff + s.ms, s.nm, bar);
 }
@@ -796,8 +805,8 @@ cudaError_t tma_prepare_kernel() {
   return ensure_smem_attr(k_fused_tma<SF, NT, NS, SCALED, STOCH>, TmaSmem<SF, NT, NS>::ALLOC, attr_done);
 }
 
-// Tensor maps of the f and g_i planes of the packed buffer `src` (bands of NT
-// cells; unused, and left empty, when a band row does not fit one box).
+// Tensor maps of the f, g_i and g_0 planes of the packed buffer `src` (bands of
+// NT cells; unused, and left empty, when a band row does not fit one box).
 template <typename SF, int NT>
 int tma_maps(const DevArgs<SF>& a, const char* src, TmaMaps& m) {
   using L = SlotLayout<SF, NT>;
@@ -807,7 +816,8 @@ int tma_maps(const DevArgs<SF>& a, const char* src, TmaMaps& m) {
   const int es = (int)sizeof(SF), box = NT + 2 * L::HF;
   const size_t pb = P.pstride * sizeof(SF);
   if (int r = encode_plane_rows(&m.f, src + P.off_f, es, a.W, a.H, 9, pb, box)) return r;
-  return encode_plane_rows(&m.gi, src + P.off_gi, es, a.W, a.H, 8, pb, box);
+  if (int r = encode_plane_rows(&m.gi, src + P.off_gi, es, a.W, a.H, 8, pb, box)) return r;
+  return encode_plane_rows(&m.g0, src + P.off_g0, 4, a.W, a.H, 1, P.off_gi - P.off_g0, NT + 2 * L::HG);
 }
 
 // Arguments of the staged kernel for one lattice with strips of R rows; the

@@ -10,11 +10,11 @@
 
 namespace fd {
 
-// The source planes of one step for the staged kernel: the nine f planes and
-// the eight g_i planes of a packed buffer, each a 3-D tensor (x, row, plane)
-// whose box is one band row of every plane.
+// The source planes of one step for the staged kernel: the nine f planes, the
+// eight g_i planes and the FP32 g_0 plane of a packed buffer, each a 3-D
+// tensor (x, row, plane) whose box is one band row of every plane.
 struct alignas(128) TmaMaps {
-  CUtensorMap f, gi;
+  CUtensorMap f, gi, g0;
 };
 
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
