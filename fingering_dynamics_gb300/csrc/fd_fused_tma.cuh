@@ -825,8 +825,9 @@ int tma_maps(const DevArgs<SF>& a, const char* src, TmaMaps& m) {
 // the resident CTAs per SM (measured on 4096 x 2048): the split ring (FP32,
 // memory-bound) loses up to 8% to a partial last wave and takes the largest
 // count that fits in three full waves (R = 29 there: 36.8 vs 34.0 GLUPS at
-// 3.1 waves); the whole-row ring (FP16/BF16, issue-bound) is best at about two
-// waves, rounded up.
+// 3.1 waves); the whole-row ring (FP16/BF16, issue-bound) is best with short
+// strips, about four waves (R = 16 there: 46.5 vs 45.7 GLUPS at two waves;
+// 12..18 rows within 1%).
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 DevArgs<SF> tma_args(const fd_params& p, const DevCoef& c, const uint16_t* mask, const double* inlet_ux, int R) {
   using M = TmaSmem<SF, NT, NS>;
@@ -849,7 +850,7 @@ DevArgs<SF> tma_args(const fd_params& p, const DevCoef& c, const uint16_t* mask,
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long slots = (long long)sms * (per_sm > 0 ? per_sm : 1);
-    long long strips = M::SPLIT ? 3 * slots / nbands : (2 * slots + nbands - 1) / nbands;
+    long long strips = M::SPLIT ? 3 * slots / nbands : (4 * slots + nbands - 1) / nbands;
     if (strips < 1) strips = 1;
     R = (int)((p.H + strips - 1) / strips);
     if (R < 16) R = 16;
