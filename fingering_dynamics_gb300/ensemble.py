@@ -98,6 +98,28 @@ def ensemble_specs(n: int, seed: int, sizes_w=(256, 512, 1024, 2048), sizes_h=(1
     return out
 
 
+def tile_count(sizes, band_width: int, rows_per_strip: int) -> int:
+    """Tiles per iteration of a batch of lattices of the given (H, W) sizes:
+    bands of `band_width` cells times strips of at most `rows_per_strip` rows."""
+    return sum(-(-W // band_width) * -(-H // min(rows_per_strip, H)) for H, W in sizes)
+
+
+def round_filling_rows(sizes, band_width: int, grid: int, max_rounds: int = 8, min_fill: float = 0.9) -> list:
+    """For each round count r = 1 .. max_rounds of a persistent grid of `grid`
+    CTAs, the shortest strips (>= 16 rows) whose tiles fit in r rounds, kept
+    when they need all r rounds and fill at least `min_fill` of them."""
+    hmax = max(H for H, _ in sizes)
+    out = []
+    for r in range(1, max_rounds + 1):
+        rows = next((h for h in range(16, hmax + 1) if tile_count(sizes, band_width, h) <= r * grid), None)
+        if rows is None:
+            continue
+        t = tile_count(sizes, band_width, rows)
+        if t > (r - 1) * grid and t >= min_fill * r * grid:
+            out.append(rows)
+    return out
+
+
 class Ensemble:
     """Independent lattices advanced by one batched launch per iteration."""
 
@@ -184,7 +206,7 @@ class Ensemble:
 
     def tiles_for(self, band_width: int, rows_per_strip: int) -> int:
         """Tiles per iteration of the shape (as fd_batch builds them)."""
-        return sum(-(-lat.W // band_width) * -(-lat.H // min(rows_per_strip, lat.H)) for lat in self.lattices)
+        return tile_count([(lat.H, lat.W) for lat in self.lattices], band_width, rows_per_strip)
 
     def wave_candidates(self, bands=(64, 128, 256), max_rounds: int = 8, min_fill: float = 0.9) -> list:
         """Shapes whose tile count just fits a whole number of rounds of the
@@ -194,20 +216,13 @@ class Ensemble:
         just over a whole number of rounds leaves a last round in which a few
         CTAs run while the others wait (up to a fifth of the launch)."""
         keep = self.config
+        sizes = [(lat.H, lat.W) for lat in self.lattices]
         out = []
-        hmax = max(lat.H for lat in self.lattices)
         for band in bands:
             self.configure(band, 64)
             grid = int(L.lib().fd_batch_grid(self._batch))
-            if grid <= 0:
-                continue
-            for r in range(1, max_rounds + 1):
-                rows = next((h for h in range(16, hmax + 1) if self.tiles_for(band, h) <= r * grid), None)
-                if rows is None:
-                    continue
-                t = self.tiles_for(band, rows)
-                if t > (r - 1) * grid and t >= min_fill * r * grid:
-                    out.append((band, rows))
+            if grid > 0:
+                out += [(band, rows) for rows in round_filling_rows(sizes, band, grid, max_rounds, min_fill)]
         if keep is not None:
             self.configure(*keep)
         return sorted(set(out))
