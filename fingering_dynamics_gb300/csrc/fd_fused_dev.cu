@@ -108,13 +108,11 @@ int fd_fused_step_packed(const fd_params* prm, const fd_storage* st, const uint1
   if (nsteps == 0) return FD_OK;
   const DevCoef c = make_dev_coef(*prm, st->f_scale_log2, st->g_scale_log2);
   cudaStream_t s = as_stream(stream);
-#ifndef FD_PACKED_REGISTER_KERNEL
   // shared-memory staged kernel: needs 16-byte aligned rows of every plane
   if (prm->W % 8 == 0) {
     const int r = fused_tma(*prm, *st, c, mask, inlet_ux, pop_a, pop_b, side_a, side_b, nsteps, rows_per_warp, s);
     return r == FD_OK ? FD_OK : check_launch("fd_fused_step_packed");
   }
-#endif
   const int R = rows_per_warp > 0 ? rows_per_warp : auto_rows_dev(prm->H, prm->W);
   float* sa = (float*)side_a;
   float* sb = (float*)side_b;
