@@ -738,6 +738,18 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const __grid_constant__ DevArg
                                        phase, ok);
 }
 
+// CTAs per SM that the batch kernel's shared memory admits (228 KB per SM, 1 KB
+// reserved per CTA, 256 B of static shared memory).  The split ring (FP32)
+// takes it as its occupancy hint, so the compiler may use the registers that
+// do not lower the occupancy (87 instead of 64 with a spill: the 96-member
+// ensemble +2%); the whole-row ring (FP16/BF16) measured 5% slower with the
+// hint and keeps the compiler's own choice (0: no hint).
+template <typename SF, int NT, int NS>
+constexpr int tma_resident_ctas() {
+  const int n = 233472 / (TmaSmem<SF, NT, NS>::ALLOC + 256 + 1024);
+  return n < 1 ? 1 : (n > 16 ? 16 : n);
+}
+
 // One lattice of a batch: its arguments and the tensor maps of its source
 // planes for both ping-pong parities (in global memory, where TMA reads them).
 template <typename SF>
@@ -760,7 +772,7 @@ struct BatchInst {
 //   ctl[2..3]  tile counter: the launch takes tiles from ctl[2+p] and one
 //              thread zeroes ctl[2+(1-p)] for the next launch.
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
-__global__ void __launch_bounds__(NT) k_fused_tma_batch(const BatchInst<SF>* __restrict__ inst,
+__global__ void __launch_bounds__(NT, (NS == 4 ? tma_resident_ctas<SF, NT, NS>() : 0)) k_fused_tma_batch(const BatchInst<SF>* __restrict__ inst,
                                                         const int4* __restrict__ tiles, int ntiles, int parity,
                                                         unsigned* __restrict__ ctl) {
   extern __shared__ __align__(128) char smem_raw[];
