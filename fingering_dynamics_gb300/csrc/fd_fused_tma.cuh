@@ -723,6 +723,18 @@ __device__ __forceinline__ void init_ring(char* smem) {
   __syncthreads();
 }
 
+// CTAs per SM that the batch kernel's shared memory admits (228 KB per SM, 1 KB
+// reserved per CTA, 256 B of static shared memory).  The split ring (FP32)
+// takes it as its occupancy hint, so the compiler may use the registers that
+// do not lower the occupancy (87 instead of 64 with a spill: the 96-member
+// ensemble +2%); the whole-row ring (FP16/BF16) measured 5% slower with the
+// hint and keeps the compiler's own choice (0: no hint).
+template <typename SF, int NT, int NS>
+constexpr int tma_resident_ctas() {
+  const int n = 233472 / (TmaSmem<SF, NT, NS>::ALLOC + 256 + 1024);
+  return n < 1 ? 1 : (n > 16 ? 16 : n);
+}
+
 // CTA b takes band b % nbands of strip strip0 + b / nbands.  `tm`: the tensor
 // maps of the step's source planes (a grid constant: TMA reads it from the
 // parameter space).
@@ -736,18 +748,6 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const __grid_constant__ DevArg
   bool ok = true;
   tma_strip<SF, NT, NS, SCALED, STOCH>(a, &tm, (int)blockIdx.x % nbands, strip0 + (int)blockIdx.x / nbands, smem,
                                        phase, ok);
-}
-
-// CTAs per SM that the batch kernel's shared memory admits (228 KB per SM, 1 KB
-// reserved per CTA, 256 B of static shared memory).  The split ring (FP32)
-// takes it as its occupancy hint, so the compiler may use the registers that
-// do not lower the occupancy (87 instead of 64 with a spill: the 96-member
-// ensemble +2%); the whole-row ring (FP16/BF16) measured 5% slower with the
-// hint and keeps the compiler's own choice (0: no hint).
-template <typename SF, int NT, int NS>
-constexpr int tma_resident_ctas() {
-  const int n = 233472 / (TmaSmem<SF, NT, NS>::ALLOC + 256 + 1024);
-  return n < 1 ? 1 : (n > 16 ? 16 : n);
 }
 
 // One lattice of a batch: its arguments and the tensor maps of its source
