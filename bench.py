@@ -349,9 +349,10 @@ def run_ours(args):
 
 
 def run_ensemble(args):
-    """BASELINE configs[2]: a seeded ensemble of independent lattices advanced
-    by one persistent batched launch per iteration (CUDA-graph replay), tile
-    shape chosen by the autotuner; aggregate MLUPS over all members."""
+    """The batched ensemble: 96 seeded independent lattices of uneven size,
+    geometry and parameters advanced by one persistent batched launch per
+    iteration (CUDA-graph replay), tile shape chosen by the autotuner;
+    aggregate MLUPS over all members."""
     import torch
     from fingering_dynamics_gb300 import build
     from fingering_dynamics_gb300.ensemble import Ensemble, ensemble_specs
@@ -452,7 +453,7 @@ def run_accelerated(args):
 
 
 def run_surrogate(args):
-    """BASELINE configs[4]: the learned surrogate at 512 x 256.  Trajectories of
+    """The learned surrogate at 512 x 256.  Trajectories of
     a seeded ensemble (batched LBM, one frame every 200 iterations), the last
     10% of geometries held out; AdamW training of the U-Net (32/64/128/256)
     with the project's tensor-core kernels, timed with CUDA events; held-out

@@ -1,6 +1,6 @@
 """CPU oracle for the two-phase (free-energy) D2Q9 lattice-Boltzmann step.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker the CUDA path is
+TEST INFRASTRUCTURE ONLY.  This module is the oracle the CUDA path is
 compared against; it is imported by ``tests/``, by ``__graft_entry__.smoke()``
 and by the CPU-baseline leg of ``bench.py`` and by nothing else.  The product
 path never calls it.

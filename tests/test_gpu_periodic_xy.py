@@ -1,7 +1,7 @@
 """The periodic-xy body-force extension on the GPU against the oracle's
 extension (tests/test_periodic_xy.py pins the oracle by exact physics; the
 reference has no such variant).  FP64 fused and per-function paths bit for
-bit, including BASELINE's small configuration at full length: 256 x 128,
+bit, including the 256 x 128 square-block configuration at full length:
 16 squares of side 10, tau 0.6 / 1.0, sigma 1e-3, 60 deg, g_x = 1e-5,
 2000 steps."""
 import numpy as np

@@ -1,6 +1,6 @@
 """The fully periodic, body-force-driven extension (variant "periodic_xy",
-BASELINE's small configuration; the reference has no such variant, so parity
-with it is unpinned).  The oracle's extension is pinned here by exact
+the 256 x 128 square-block configuration; the reference has no such variant,
+so parity with it is unpinned).  The oracle's extension is pinned here by exact
 physics: Guo forcing adds exactly rho g of momentum per cell and step, and a
 periodic lattice without obstacles conserves both colour masses."""
 import numpy as np
