@@ -286,8 +286,8 @@ def run_ours(args):
     e2e_s = float("nan")
 
     def host_step(host):
-        if lat.storage is not None:
-            lat.advance_host(host)
+        if lat.storage is not None and not args.e2e_serial:
+            lat.advance_host(host, chunk_rows=args.e2e_chunk_rows)
         else:
             lat.upload_populations(host)
             lat.advance(1, args.rows)
@@ -334,7 +334,9 @@ def run_ours(args):
                          "algorithmic_bytes_per_launch": alg_bytes},
             "e2e": None if args.no_e2e else {
                 "value": round(world * cells * e2e_steps / e2e_s / 1e6, 1), "unit": "MLUPS",
-                "h2d_bytes_per_step": pop_bytes, "d2h_bytes_per_step": pop_bytes},
+                "h2d_bytes_per_step": pop_bytes, "d2h_bytes_per_step": pop_bytes,
+                "path": "serial" if (args.e2e_serial or lat.storage is None) else
+                        f"pipelined host step, chunk rows {args.e2e_chunk_rows or 'auto'}"},
             "gpu_launches": args.steps,
             "clocks": clocks,
             # fluid cells only (the metric counts every cell, solid ones too, as the reference streams them)
@@ -593,6 +595,10 @@ def main():
     ap.add_argument("--rows", type=int, default=0, help="rows per warp (0 = automatic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end measurement")
+    ap.add_argument("--e2e-chunk-rows", type=int, default=0,
+                    help="e2e: rows per chunk of the pipelined host step (0: automatic)")
+    ap.add_argument("--e2e-serial", action="store_true",
+                    help="e2e: upload, step and download one after the other instead of the pipelined host step")
     ap.add_argument("--H", type=int, default=H_FULL, help="lattice rows (default: the 4096 x 2048 workload)")
     ap.add_argument("--W", type=int, default=W_FULL, help="lattice columns")
     ap.add_argument("--workload", default="single",
