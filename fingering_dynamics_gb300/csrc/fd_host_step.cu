@@ -22,6 +22,7 @@
 
 #include "fd_fused_dev.cuh"
 #include "fd_host.h"
+#include "fd_host_plan.h"
 
 namespace fd {
 
@@ -30,9 +31,6 @@ int fused_tma_strips(const fd_params& p, const fd_storage& st, const DevCoef& c,
                      int strip0, int nstrips, uint32_t seed, cudaStream_t s);
 
 namespace {
-
-constexpr int kStripRows = 16;   // strip height of the chunked launches
-constexpr int kMaxChunks = 256;  // chunks per call (bounds the events in use)
 
 // Streams and events of the pipeline, one set per device, created on first
 // use and kept for the life of the process.  Calls on one device serialise on
@@ -98,9 +96,8 @@ cudaError_t copy_rows(const Planes& q, int W, int r0, int r1, char* dst, const c
 
 // Enqueue the uploads, the iterations and the downloads (after the fork).
 int host_pipeline(Pipe& pipe, const fd_params& prm, const fd_storage& st, const DevCoef& coef, const uint16_t* mask,
-                  const double* inlet_ux, const Planes& q, const std::vector<int>& cb, const std::vector<int>& order,
-                  int R, int nstrips, int nsteps, const char* hin, char* hout, char* pa, char* pb, float* sa,
-                  float* sb, cudaStream_t s);
+                  const double* inlet_ux, const Planes& q, const HostPlan& plan, int nsteps, const char* hin,
+                  char* hout, char* pa, char* pb, float* sa, float* sb, cudaStream_t s);
 
 }  // namespace
 }  // namespace fd
@@ -128,24 +125,7 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
   if (cudaGetDevice(&dev) != cudaSuccess) return check_launch("fd_fused_step_packed_host");
   FD_REQUIRE(dev >= 0 && dev < 64, FD_ERR_ARG, "fd_fused_step_packed_host: device ordinal %d", dev);
 
-  const int H = prm->H;
-  const int R = H < kStripRows ? H : kStripRows;
-  const int nstrips = (H + R - 1) / R;
-  // chunks of m strips (about 16 chunks unless the caller asks otherwise)
-  // after a ramp of 1, 1, 2, 4 strips; chunk c = strips cb[c] .. cb[c+1]-1
-  int m = chunk_rows > 0 ? (chunk_rows + R - 1) / R : (nstrips + 15) / 16;
-  if (m < 1) m = 1;
-  if ((nstrips + m - 1) / m > kMaxChunks - 4) m = (nstrips + kMaxChunks - 5) / (kMaxChunks - 4);
-  std::vector<int> cb{0};
-  for (int sz : {1, 1, 2, 4})
-    if (cb.back() < nstrips) cb.push_back(std::min(cb.back() + std::min(sz, m), nstrips));
-  while (cb.back() < nstrips) cb.push_back(std::min(cb.back() + m, nstrips));
-  const int K = (int)cb.size() - 1;
-  // compute order: chunks whose neighbours do not wrap first
-  std::vector<int> order;
-  for (int c = 1; c + 1 < K; ++c) order.push_back(c);
-  if (K > 1) order.push_back(K - 1);
-  order.push_back(0);
+  const HostPlan plan = host_plan(prm->H, chunk_rows);
 
   const Planes q = planes_of(*prm, st->dtype);
   const DevCoef coef = make_dev_coef(*prm, st->f_scale_log2, st->g_scale_log2);
@@ -165,8 +145,7 @@ extern "C" int fd_fused_step_packed_host(const fd_params* prm, const fd_storage*
   if (cudaEventRecord(pipe.fork, s) != cudaSuccess || cudaStreamWaitEvent(pipe.up, pipe.fork, 0) != cudaSuccess ||
       cudaStreamWaitEvent(pipe.down, pipe.fork, 0) != cudaSuccess)
     return check_launch("fd_fused_step_packed_host: fork");
-  const int r = host_pipeline(pipe, *prm, *st, coef, mask, inlet_ux, q, cb, order, R, nstrips, nsteps, hin, hout, pa,
-                              pb, sa, sb, s);
+  const int r = host_pipeline(pipe, *prm, *st, coef, mask, inlet_ux, q, plan, nsteps, hin, hout, pa, pb, sa, sb, s);
   // join, also after a failure: the caller's stream continues after the
   // copies already issued on both internal streams
   const bool joined = cudaEventRecord(pipe.up_done, pipe.up) == cudaSuccess &&
@@ -182,10 +161,10 @@ namespace fd {
 namespace {
 
 int host_pipeline(Pipe& pipe, const fd_params& prm, const fd_storage& st, const DevCoef& coef, const uint16_t* mask,
-                  const double* inlet_ux, const Planes& q, const std::vector<int>& cb, const std::vector<int>& order,
-                  int R, int nstrips, int nsteps, const char* hin, char* hout, char* pa, char* pb, float* sa,
-                  float* sb, cudaStream_t s) {
-  const int K = (int)cb.size() - 1, H = prm.H, W = prm.W;
+                  const double* inlet_ux, const Planes& q, const HostPlan& plan, int nsteps, const char* hin,
+                  char* hout, char* pa, char* pb, float* sa, float* sb, cudaStream_t s) {
+  const std::vector<int>& cb = plan.cb;
+  const int K = (int)cb.size() - 1, H = prm.H, W = prm.W, R = plan.R, nstrips = plan.nstrips;
   auto rows_of = [&](int c, int& r0, int& r1) {
     r0 = cb[c] * R;
     r1 = std::min(cb[c + 1] * R, H);
@@ -210,10 +189,9 @@ int host_pipeline(Pipe& pipe, const fd_params& prm, const fd_storage& st, const 
         return r;
       continue;
     }
-    for (int c : order) {
+    for (int c : plan.order) {
       if (first) {
-        const int need = (c >= 1 && c + 1 < K) ? c + 1 : K - 1;  // last chunk whose rows chunk c reads
-        if (cudaStreamWaitEvent(s, pipe.ev_up[need], 0) != cudaSuccess)
+        if (cudaStreamWaitEvent(s, pipe.ev_up[plan.need[c]], 0) != cudaSuccess)
           return check_launch("fd_fused_step_packed_host: wait for upload");
       }
       const int s0 = cb[c], ns = cb[c + 1] - cb[c];
