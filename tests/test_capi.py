@@ -67,3 +67,35 @@ def test_package_fails_loudly_without_library(monkeypatch):
     monkeypatch.setattr(L, "LIB_PATH", "/nonexistent/libfdlbm.so")
     with pytest.raises(RuntimeError, match="not built"):
         L.lib()
+
+
+def test_new_entry_points_check_their_arguments_on_the_host(lib):
+    """The host-resident step, the batch grid query and the wait self-test
+    reject bad arguments before touching the device."""
+    from fingering_dynamics_gb300 import _lib as L
+    prm = L.fd_params(64, 64, 1, 0, 0.8, 0.1, 2.0, -0.01, 0.01, 1.0, 0.0, 1.5)
+    st = L.fd_storage(L.FD_F32, 0, 0, 0, 0)
+    with pytest.raises(L.FDError) as e:  # NULL buffers
+        L.call("fd_fused_step_packed_host", ctypes.byref(prm), ctypes.byref(st), None, None, None, None, None, None,
+               None, None, 1, 0, None)
+    assert e.value.code == -1 and "NULL" in str(e.value)
+    dummy = ctypes.c_void_p(256)
+    with pytest.raises(L.FDError) as e:  # no iteration to run
+        L.call("fd_fused_step_packed_host", ctypes.byref(prm), ctypes.byref(st), dummy, dummy, dummy, dummy,
+               ctypes.c_void_p(512), ctypes.c_void_p(768), ctypes.c_void_p(1024), ctypes.c_void_p(1280), 0, 0, None)
+    assert e.value.code == -1
+    prm.W = 60  # not a multiple of 8
+    with pytest.raises(L.FDError) as e:
+        L.call("fd_fused_step_packed_host", ctypes.byref(prm), ctypes.byref(st), dummy, dummy, dummy, dummy,
+               ctypes.c_void_p(512), ctypes.c_void_p(768), ctypes.c_void_p(1024), ctypes.c_void_p(1280), 1, 0, None)
+    assert e.value.code == -2
+    st.rounding = 7  # unknown rounding
+    prm.W = 64
+    with pytest.raises(L.FDError):
+        L.call("fd_fused_step_packed_host", ctypes.byref(prm), ctypes.byref(st), dummy, dummy, dummy, dummy,
+               ctypes.c_void_p(512), ctypes.c_void_p(768), ctypes.c_void_p(1024), ctypes.c_void_p(1280), 1, 0, None)
+    assert L.lib().fd_batch_grid(None) == -1 and L.lib().fd_batch_tiles(None) == -1
+    for polls, unit in ((0, 0), (1 << 21, 0), (100, 2)):
+        with pytest.raises(L.FDError) as e:
+            L.call("fd_selftest_wait_timeout", polls, unit, None)
+        assert e.value.code == -1
