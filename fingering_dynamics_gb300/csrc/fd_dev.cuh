@@ -118,17 +118,75 @@ struct DevMacro {
   float drho, rho, ux, uy, psi, mu, gx, gy, inv_tau, pref;
 };
 
-__device__ __forceinline__ DevMacro dev_macros(const DevCoef& c, const float (&d)[9], float psi, float gx, float gy,
-                                               float lap) {
+// ---- psi and its stencils -------------------------------------------------
+// psi = sum of g (fingering_periodic.py:210-212) as the unevaluated sum hi + lo
+// of two floats: hi = fl(g_0 + S) with S = g_1 + .. + g_8 (small), lo = the
+// rounding error of that addition, exact by the TwoSum algorithm (Knuth, TAOCP
+// vol. 2, 4.2.2).  Near the pure phases psi is close to +-1, where one float
+// resolves it to 6e-8 only; the stencils below take differences of
+// neighbouring psi values and the free energy takes 1 - psi^2, both of which
+// lose that resolution to cancellation when psi is a single float.
+__device__ __forceinline__ float2 dev_psi_pair(const float (&g)[9]) {
+  const float S = ((g[1] + g[2]) + (g[3] + g[4])) + ((g[5] + g[6]) + (g[7] + g[8]));
+  const float hi = g[0] + S;
+  const float b = hi - g[0];
+  const float lo = (g[0] - (hi - b)) + (S - b);
+  return make_float2(hi, lo);
+}
+
+// d(psi)/dx, d(psi)/dy and the laplacian of the 3x3 neighbourhood
+// (fingering_periodic.py:214-256), and the factor 1 - psi^2 of the bulk free
+// energy (fingering_periodic.py:141-144).
+struct DevStencil {
+  float gx, gy, lap, psi, omp;
+};
+
+// Single-float psi (FP16/BF16 storage, whose own resolution is far coarser).
+__device__ __forceinline__ DevStencil dev_stencil(float C, float E, float Wv, float N, float S, float NE, float NW,
+                                                  float SE, float SW) {
+  DevStencil s;
+  s.gx = (4.0f * (E - Wv) + ((NE - NW) + (SE - SW))) * (1.0f / 12.0f);
+  s.gy = (4.0f * (N - S) + ((NE - SE) + (NW - SW))) * (1.0f / 12.0f);
+  s.lap = (4.0f * ((N + S) + (E + Wv)) + ((NE + NW) + (SE + SW)) - 20.0f * C) * (1.0f / 6.0f);
+  s.psi = C;
+  s.omp = fmaf(-C, C, 1.0f);
+  return s;
+}
+
+// Paired psi (FP32 storage): every neighbour enters as its difference from the
+// centre, (hi_n - hi_c) + (lo_n - lo_c), where hi_n - hi_c is exact for close
+// values; 1 - psi^2 = ((1 - hi) - lo) ((1 + hi) + lo).
+__device__ __forceinline__ DevStencil dev_stencil_pair(float2 C, float2 E, float2 Wv, float2 N, float2 S, float2 NE,
+                                                       float2 NW, float2 SE, float2 SW) {
+  auto df = [&](float2 v) { return (v.x - C.x) + (v.y - C.y); };
+  const float dE = df(E), dW = df(Wv), dN = df(N), dS = df(S);
+  const float dNE = df(NE), dNW = df(NW), dSE = df(SE), dSW = df(SW);
+  DevStencil s;
+  s.gx = (4.0f * (dE - dW) + ((dNE - dNW) + (dSE - dSW))) * (1.0f / 12.0f);
+  s.gy = (4.0f * (dN - dS) + ((dNE - dSE) + (dNW - dSW))) * (1.0f / 12.0f);
+  s.lap = (4.0f * ((dN + dS) + (dE + dW)) + ((dNE + dNW) + (dSE + dSW))) * (1.0f / 6.0f);
+  s.psi = C.x + C.y;
+  s.omp = ((1.0f - C.x) - C.y) * ((1.0f + C.x) + C.y);
+  return s;
+}
+
+// getMu_plain (fingering_periodic.py:146-149) of a stencil, the Zou-He input
+// stored in the boundary-value buffer
+__device__ __forceinline__ float dev_mu(const DevCoef& c, const DevStencil& s) {
+  return c.a * s.psi * s.omp - c.kappa * s.lap;
+}
+
+__device__ __forceinline__ DevMacro dev_macros(const DevCoef& c, const float (&d)[9], const DevStencil& st) {
   DevMacro m;
   m.drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
   m.rho = 1.0f + m.drho;
   const float jx = ((d[1] - d[3]) + (d[5] - d[6])) + (d[8] - d[7]);
   const float jy = ((d[2] - d[4]) + (d[5] - d[8])) + (d[6] - d[7]);
+  const float psi = st.psi, gx = st.gx, gy = st.gy;
   m.psi = psi;
   m.gx = gx;
   m.gy = gy;
-  m.mu = c.a * psi * (1.0f - psi * psi) - c.kappa * lap;  // getMu (fingering_periodic.py:141-144)
+  m.mu = dev_mu(c, st);  // getMu (fingering_periodic.py:141-144)
   const float inv_rho = __frcp_rn(m.rho);
   m.ux = fmaf(0.5f * m.mu, gx, jx) * inv_rho;             // getUx (fingering_periodic.py:126-132)
   m.uy = fmaf(0.5f * m.mu, gy, jy) * inv_rho;
@@ -279,27 +337,29 @@ __device__ __forceinline__ void dev_zou_he_f(const DevCoef& c, int variant, int 
 
 __device__ __forceinline__ void dev_zou_he_g(const DevCoef& c, int variant, int H, int W, int x, int y, float (&g)[9]) {
   if (x == 0) {
+    // 1 - g_0 (and -1 - g_0 at the outlet) first: g_0 is close to +1 (-1) there, so
+    // the difference is exact and the small populations are not rounded against 1
     if (variant == FD_VARIANT_WALLS && y == 0) {
       g[1] = g[3];
       g[2] = g[4];
       g[5] = g[7];
-      g[6] = (1.0f / 36.0f) * (1.0f - (((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + g[7]))) * 18.0f;
+      g[6] = 0.5f * ((1.0f - g[0]) - (((g[1] + g[2]) + (g[3] + g[4])) + (g[5] + g[7])));  // w6 / (w6 + w8)
       g[8] = g[6];
     } else if (variant == FD_VARIANT_WALLS && y == H - 1) {
       g[1] = g[3];
       g[4] = g[2];
       g[8] = g[6];
-      g[5] = (1.0f / 36.0f) * (1.0f - (((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[6]) + g[8]))) * 18.0f;
+      g[5] = 0.5f * ((1.0f - g[0]) - (((g[1] + g[2]) + (g[3] + g[4])) + (g[6] + g[8])));
       g[7] = g[5];
     } else {
-      const float psi_in = 1.0f - ((((g[0] + g[2]) + (g[3] + g[4])) + g[6]) + g[7]);
+      const float psi_in = (1.0f - g[0]) - (((g[2] + g[3]) + (g[4] + g[6])) + g[7]);
       g[1] = (2.0f / 3.0f) * psi_in;   // w1 / (w1 + w5 + w8)
       g[5] = (1.0f / 6.0f) * psi_in;
       g[8] = (1.0f / 6.0f) * psi_in;
     }
   }
   if (x == W - 1) {
-    const float psi_out = -1.0f - ((((g[0] + g[1]) + (g[2] + g[4])) + g[5]) + g[8]);
+    const float psi_out = (-1.0f - g[0]) - (((g[1] + g[2]) + (g[4] + g[5])) + g[8]);
     g[3] = (2.0f / 3.0f) * psi_out;
     g[6] = (1.0f / 6.0f) * psi_out;
     g[7] = (1.0f / 6.0f) * psi_out;

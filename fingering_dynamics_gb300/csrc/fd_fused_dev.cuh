@@ -160,9 +160,11 @@ __device__ __forceinline__ void pull_g_row(const DevArgs<SF>& a, int y, int xw, 
   }
 }
 
+// psi of the row's cells: the pair (hi, lo) of dev_psi_pair for FP32 storage,
+// else (psi, 0) (see the staged kernel's psi_paired).
 template <typename SF, int VEC>
 __device__ __forceinline__ void g_row_dev(const DevArgs<SF>& a, int y, int x0, int xw, uint16_t (&mb)[VEC],
-                                          float (&g)[9][VEC], float (&psi)[VEC]) {
+                                          float (&g)[9][VEC], float2 (&psi)[VEC]) {
   ld_vec<uint16_t, VEC>(a.mask + (size_t)y * a.W + xw, mb);
   pull_g_row<SF, VEC>(a, y, xw, mb, g);
   if (x0 == 0) {
@@ -184,8 +186,19 @@ __device__ __forceinline__ void g_row_dev(const DevArgs<SF>& a, int y, int x0, i
 #pragma unroll
   for (int k = 0; k < VEC; ++k) {
     const int x = x0 + k;
-    const float s = ((g[0][k] + g[1][k]) + (g[2][k] + g[3][k])) + ((g[4][k] + g[5][k]) + (g[6][k] + g[7][k])) + g[8][k];
-    psi[k] = (x < 0) ? 1.0f : (x >= a.W) ? -1.0f : ((mb[k] & SOLID) ? a.c.psi_wall : s);
+    float gc[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) gc[i] = g[i][k];
+    float2 s;
+    if constexpr (std::is_same_v<SF, float>) {
+      s = dev_psi_pair(gc);
+    } else {
+      const float S = ((gc[1] + gc[2]) + (gc[3] + gc[4])) + ((gc[5] + gc[6]) + (gc[7] + gc[8]));
+      s = make_float2(gc[0] + S, 0.0f);
+    }
+    psi[k] = (x < 0) ? make_float2(1.0f, 0.0f)
+                     : (x >= a.W) ? make_float2(-1.0f, 0.0f)
+                                  : ((mb[k] & SOLID) ? make_float2(a.c.psi_wall, 0.0f) : s);
   }
 }
 
@@ -210,8 +223,7 @@ __device__ __forceinline__ float dev_rho_inlet_row(const DevArgs<SF>& a, int yn)
 
 template <typename SF, int VEC, int K>
 __device__ __forceinline__ void dev_boundary_cell(const DevArgs<SF>& a, int y, int x, float (&f)[9][VEC],
-                                                  const float (&gx)[VEC], const float (&gy)[VEC],
-                                                  const float (&lap)[VEC], const float (&Pc)[VEC]) {
+                                                  const DevStencil (&st)[VEC]) {
   const int o = (x == 0) ? 0 : 3;
   float drho_nb = 0.0f;
   if (a.variant == FD_VARIANT_WALLS && x == 0 && (y == 0 || y == a.H - 1))
@@ -223,17 +235,17 @@ __device__ __forceinline__ void dev_boundary_cell(const DevArgs<SF>& a, int y, i
                a.side_in[(o + 1) * a.H + y], a.side_in[(o + 2) * a.H + y], drho_nb);
 #pragma unroll
   for (int i = 0; i < 9; ++i) f[i][K] = fc[i];
-  a.side_out[(o + 0) * a.H + y] = gx[K];
-  a.side_out[(o + 1) * a.H + y] = gy[K];
-  a.side_out[(o + 2) * a.H + y] = a.c.a * Pc[K] * (1.0f - Pc[K] * Pc[K]) - a.c.kappa * lap[K];
+  a.side_out[(o + 0) * a.H + y] = st[K].gx;
+  a.side_out[(o + 1) * a.H + y] = st[K].gy;
+  a.side_out[(o + 2) * a.H + y] = dev_mu(a.c, st[K]);
 }
 
 template <int VEC>
-__device__ __forceinline__ void extend_f(const float (&p)[VEC], float (&e)[VEC + 2]) {
-  e[0] = __shfl_up_sync(0xffffffffu, p[VEC - 1], 1);
+__device__ __forceinline__ void extend_f(const float2 (&p)[VEC], float2 (&e)[VEC + 2]) {
+  e[0] = make_float2(__shfl_up_sync(0xffffffffu, p[VEC - 1].x, 1), __shfl_up_sync(0xffffffffu, p[VEC - 1].y, 1));
 #pragma unroll
   for (int k = 0; k < VEC; ++k) e[k + 1] = p[k];
-  e[VEC + 1] = __shfl_down_sync(0xffffffffu, p[0], 1);
+  e[VEC + 1] = make_float2(__shfl_down_sync(0xffffffffu, p[0].x, 1), __shfl_down_sync(0xffffffffu, p[0].y, 1));
 }
 
 #ifndef FD_DEV_MINB
@@ -279,12 +291,12 @@ __global__ void __launch_bounds__(128, FD_DEV_MINB) k_fused_dev(const DevArgs<SF
   const bool walls = a.variant == FD_VARIANT_WALLS;
 
   float gC[9][VEC], gN[9][VEC];
-  float Pm[VEC], Pc[VEC], Pn[VEC];
+  float2 Pm[VEC], Pc[VEC], Pn[VEC];
   uint16_t mC[VEC], mN[VEC];
 
   if (walls && y0 == 0) {
 #pragma unroll
-    for (int k = 0; k < VEC; ++k) Pm[k] = a.c.psi_wall;
+    for (int k = 0; k < VEC; ++k) Pm[k] = make_float2(a.c.psi_wall, 0.0f);
   } else {
     g_row_dev<SF, VEC>(a, wrap(y0 - 1, a.H), x0, xw, mN, gN, Pm);
   }
@@ -295,34 +307,35 @@ __global__ void __launch_bounds__(128, FD_DEV_MINB) k_fused_dev(const DevArgs<SF
       prefetch_rows(a, lane, chunk, wrap(y + 1 + FD_DEV_PREFETCH, a.H), wrap(y + 2 + FD_DEV_PREFETCH, a.H));
     if (walls && y + 1 >= a.H) {
 #pragma unroll
-      for (int k = 0; k < VEC; ++k) Pn[k] = a.c.psi_wall;
+      for (int k = 0; k < VEC; ++k) Pn[k] = make_float2(a.c.psi_wall, 0.0f);
     } else {
       g_row_dev<SF, VEC>(a, wrap(y + 1, a.H), x0, xw, mN, gN, Pn);
     }
-    float em[VEC + 2], ec[VEC + 2], en[VEC + 2];
+    float2 em[VEC + 2], ec[VEC + 2], en[VEC + 2];
     extend_f<VEC>(Pm, em);
     extend_f<VEC>(Pc, ec);
     extend_f<VEC>(Pn, en);
-    float gx[VEC], gy[VEC], lap[VEC];
+    DevStencil st[VEC];
 #pragma unroll
     for (int k = 0; k < VEC; ++k) {
-      const float E = ec[k + 2], Wv = ec[k], N = en[k + 1], S = em[k + 1];
-      const float NE = en[k + 2], NW = en[k], SE = em[k + 2], SW = em[k];
-      gx[k] = (4.0f * (E - Wv) + ((NE - NW) + (SE - SW))) * (1.0f / 12.0f);
-      gy[k] = (4.0f * (N - S) + ((NE + NW) - (SE + SW))) * (1.0f / 12.0f);
-      lap[k] = (4.0f * ((N + S) + (E + Wv)) + ((NE + NW) + (SE + SW)) - 20.0f * ec[k + 1]) * (1.0f / 6.0f);
+      if constexpr (std::is_same_v<SF, float>)
+        st[k] = dev_stencil_pair(ec[k + 1], ec[k + 2], ec[k], en[k + 1], em[k + 1], en[k + 2], en[k], em[k + 2],
+                                 em[k]);
+      else
+        st[k] = dev_stencil(ec[k + 1].x, ec[k + 2].x, ec[k].x, en[k + 1].x, em[k + 1].x, en[k + 2].x, en[k].x,
+                            em[k + 2].x, em[k].x);
     }
     float f[9][VEC];
     pull_f_row<SF, VEC>(a, y, xw, mC, f);
-    if (owned && x0 == 0) dev_boundary_cell<SF, VEC, 0>(a, y, 0, f, gx, gy, lap, Pc);
-    if (owned && x0 == a.W - VEC) dev_boundary_cell<SF, VEC, VEC - 1>(a, y, a.W - 1, f, gx, gy, lap, Pc);
+    if (owned && x0 == 0) dev_boundary_cell<SF, VEC, 0>(a, y, 0, f, st);
+    if (owned && x0 == a.W - VEC) dev_boundary_cell<SF, VEC, VEC - 1>(a, y, a.W - 1, f, st);
 #pragma unroll
     for (int k = 0; k < VEC; ++k) {
       if (!(mC[k] & SOLID)) {
         float fc[9], gc[9];
 #pragma unroll
         for (int i = 0; i < 9; ++i) { fc[i] = f[i][k]; gc[i] = gC[i][k]; }
-        const DevMacro m = dev_macros(a.c, fc, Pc[k], gx[k], gy[k], lap[k]);
+        const DevMacro m = dev_macros(a.c, fc, st[k]);
         dev_collide(a.c, m, fc, gc);
 #pragma unroll
         for (int i = 0; i < 9; ++i) { f[i][k] = fc[i]; gC[i][k] = gc[i]; }

@@ -54,6 +54,16 @@ constexpr int tma_ring_depth() {
   return std::is_same_v<SF, float> ? FD_TMA_NS_F32 : FD_TMA_NS_16;
 }
 
+// FP32 storage carries psi as a float pair hi + lo (fd_dev.cuh, dev_psi_pair)
+// through the psi ring; the lo parts (at most half an ulp of hi) are kept as
+// FP16 scaled by 2^24, whose 11-bit significand leaves an error below 1e-11.
+template <typename SF>
+constexpr bool psi_paired() {
+  return std::is_same_v<SF, float>;
+}
+constexpr float kPsiLoScale = 16777216.0f;          // 2^24
+constexpr float kPsiLoInv = 1.0f / 16777216.0f;
+
 // Device-side error word: bit 0 = an mbarrier wait gave up (copy never
 // completed).  The library is built without relocatable device code, so every
 // translation unit that includes this header has its own copy, read and
@@ -146,7 +156,10 @@ struct SlotLayout {
 // (f, g and mask of a row behind one mbarrier).  NS == 4: the split ring, four
 // slots whose f half and g half complete on separate mbarriers (0..3: g half
 // and mask row, 4..7: f half), without the mask; the mask rows live in a ring
-// of their own (8 rows) and arrive with the g half.
+// of their own and arrive with the g half (6 rows: row r arrives at the
+// barrier of row r - 4 and is last read by the f pull of row r).  The psi ring
+// holds 4 rows of NT + 2 floats, plus their FP16 lo parts when psi is paired;
+// with the 6-row mask ring the FP32 split ring still fits five CTAs per SM.
 template <typename SF, int NT, int NS>
 struct TmaSmem {
   using L = SlotLayout<SF, NT>;
@@ -155,8 +168,9 @@ struct TmaSmem {
   static constexpr int PSI_ROW = NT + 2;
   static constexpr int OFF_BAR = 0;
   static constexpr int OFF_PSI = 128;
-  static constexpr int OFF_MASK = (OFF_PSI + 4 * PSI_ROW * 4 + 127) / 128 * 128;
-  static constexpr int MASK_ROWS = SPLIT ? 8 : 0;
+  static constexpr int OFF_PLO = OFF_PSI + 4 * PSI_ROW * 4;
+  static constexpr int OFF_MASK = (OFF_PLO + (psi_paired<SF>() ? 4 * PSI_ROW * 2 : 0) + 127) / 128 * 128;
+  static constexpr int MASK_ROWS = SPLIT ? 6 : 0;
   static constexpr int OFF_SLOT = (OFF_MASK + MASK_ROWS * L::RM + 127) / 128 * 128;
   static constexpr int SLOT = SPLIT ? (L::OFF_M + 127) / 128 * 128 : L::BYTES;
   static constexpr int BYTES = OFF_SLOT + NS * SLOT;
@@ -321,16 +335,56 @@ __device__ __forceinline__ unsigned mask_at(const char* sm, int mrow, int lx) {
 // psi of cell x (band index lx) of row y from its pulled g after Zou-He
 // (fingering_periodic.py:210-212, 278-302); the pulled g is returned in g.
 // `mrow` is the byte offset of row y's mask row.
+// With paired psi (psi_paired) the result is the pair (hi, lo), else (psi, 0).
 template <typename SF, int NT, bool SCALED>
-__device__ __forceinline__ float psi_cell(const char* sm, const DevArgs<SF>& a, const int (&rows)[3], int mrow, int x,
-                                          int lx, int y, float (&g)[9]) {
-  if (x < 0) return 1.0f;
-  if (x >= a.W) return -1.0f;
+__device__ __forceinline__ float2 psi_cell(const char* sm, const DevArgs<SF>& a, const int (&rows)[3], int mrow, int x,
+                                           int lx, int y, float (&g)[9]) {
+  if (x < 0) return make_float2(1.0f, 0.0f);
+  if (x >= a.W) return make_float2(-1.0f, 0.0f);
   const unsigned m = mask_at<SF, NT>(sm, mrow, lx);
   pull_cell<SF, NT, true, SCALED>(sm, a.c, rows, lx, m & 0xFFu, g);
   if (x == 0 || x == a.W - 1) dev_zou_he_g(a.c, a.variant, a.H, a.W, x, y, g);
-  if (m & SOLID) return a.c.psi_wall;
-  return ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+  if (m & SOLID) return make_float2(a.c.psi_wall, 0.0f);
+  if constexpr (psi_paired<SF>()) {
+    return dev_psi_pair(g);
+  } else {
+    const float S = ((g[1] + g[2]) + (g[3] + g[4])) + ((g[5] + g[6]) + (g[7] + g[8]));
+    return make_float2(g[0] + S, 0.0f);
+  }
+}
+
+// The psi ring (4 rows of NT + 2 cells, hi parts as floats, lo parts as scaled
+// FP16 when psi is paired).  `row` is the element offset of a ring row.
+template <typename SF, int NT, int NS>
+struct PsiRing {
+  float* hi;
+  __half* lo;
+  __device__ __forceinline__ explicit PsiRing(char* smem)
+      : hi(reinterpret_cast<float*>(smem + TmaSmem<SF, NT, NS>::OFF_PSI)),
+        lo(reinterpret_cast<__half*>(smem + TmaSmem<SF, NT, NS>::OFF_PLO)) {}
+  __device__ __forceinline__ void put(int row, int j, float2 v) const {
+    hi[row + j] = v.x;
+    if constexpr (psi_paired<SF>()) lo[row + j] = __float2half_rn(v.y * kPsiLoScale);
+  }
+  __device__ __forceinline__ float2 get(int row, int j) const {
+    if constexpr (psi_paired<SF>()) return make_float2(hi[row + j], __half2float(lo[row + j]) * kPsiLoInv);
+    else return make_float2(hi[row + j], 0.0f);
+  }
+};
+
+// Stencils of cell j of the psi ring row `pc` (rows pm and pn below and
+// above); the cell's own column comes from registers (S, C, N).
+template <typename SF, int NT, int NS>
+__device__ __forceinline__ DevStencil ring_stencil(const PsiRing<SF, NT, NS>& ring, int pm, int pc, int pn, int j,
+                                                   float2 S, float2 C, float2 N) {
+  if constexpr (psi_paired<SF>()) {
+    return dev_stencil_pair(C, ring.get(pc, j + 1), ring.get(pc, j - 1), N, S, ring.get(pn, j + 1),
+                            ring.get(pn, j - 1), ring.get(pm, j + 1), ring.get(pm, j - 1));
+  } else {
+    const float* h = ring.hi;
+    return dev_stencil(C.x, h[pc + j + 1], h[pc + j - 1], N.x, S.x, h[pn + j + 1], h[pn + j - 1], h[pm + j + 1],
+                       h[pm + j - 1]);
+  }
 }
 
 // One strip of one band: the body shared by the single-lattice kernel and the
@@ -344,7 +398,8 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
   using L = SlotLayout<SF, NT>;
   using M = TmaSmem<SF, NT, NS>;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
-  float* psi_ring = reinterpret_cast<float*>(smem + M::OFF_PSI);
+  const PsiRing<SF, NT, NS> ring(smem);
+  const float2 wallv = make_float2(a.c.psi_wall, 0.0f);
 
   const int t = threadIdx.x;
   const int x0 = band * NT;
@@ -375,10 +430,10 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
     so[k] = M::OFF_SLOT + k * M::SLOT;
   }
   int pslot = 0;  // psi ring slot of row y0-1; rows y0-1, y0, y0+1 use pslot, +1, +2 (mod 4)
-  auto psi_row = [&](int k) { return psi_ring + ((pslot + k) & 3) * M::PSI_ROW; };
+  auto psi_row = [&](int k) { return ((pslot + k) & 3) * M::PSI_ROW; };
 
   float gC[9], gN[9];
-  float pS = 0.0f, pC = 0.0f;  // psi of this column at rows y-1 and y
+  float2 pS = wallv, pC = wallv;  // psi of this column at rows y-1 and y
   // prologue: psi of rows y0-1 and y0 (needs rows y0-2 .. y0+1)
   wait_slot(0);
   wait_slot(1);
@@ -388,16 +443,17 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
   for (int k = 0; k < 2; ++k) {
     const int r = y0 - 1 + k;
     const int rows[3] = {so[k], so[k + 1], so[k + 2]};
-    float* pr = psi_row(k);
+    const int pr = psi_row(k);
     const bool ghost = walls && (r < 0 || r >= a.H);
     const int yr = wrap(r, a.H);
-    const float pv = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x, t, yr, gN);
-    pr[t + 1] = pv;
+    const float2 pv = ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x, t, yr, gN);
+    ring.put(pr, t + 1, pv);
     if (k == 0) pS = pv;
     else pC = pv;
     if (halo) {
       float gh[9];
-      pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x0 + hl, hl, yr, gh);
+      ring.put(pr, hl + 1,
+               ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x0 + hl, hl, yr, gh));
     }
   }
 #pragma unroll
@@ -405,18 +461,19 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
 
   for (int y = y0; y < y1; ++y) {
     // 1. psi of row y+1 from rows y, y+1, y+2
-    float pN;
+    float2 pN;
     wait_slot(si[4]);
     {
       const int rows[3] = {so[2], so[3], so[4]};
       const bool ghost = walls && (y + 1 >= a.H);
       const int yr = wrap(y + 1, a.H);
-      float* pr = psi_row(2);
-      pN = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x, t, yr, gN);
-      pr[t + 1] = pN;
+      const int pr = psi_row(2);
+      pN = ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x, t, yr, gN);
+      ring.put(pr, t + 1, pN);
       if (halo) {
         float gh[9];
-        pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x0 + hl, hl, yr, gh);
+        ring.put(pr, hl + 1,
+                 ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, rows[1] + L::OFF_M, x0 + hl, hl, yr, gh));
       }
     }
     // rho_inlet - 1 of row 1 (bottom inlet corner, rows 0..2 = y..y+2) or of
@@ -435,15 +492,7 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
     if (t == 0 && y + NS - 2 <= last) issue_row<SF, NT>(a, tm, smem + so[0], &bars[si[0]], y + NS - 2, x0);
     // 3. stencils, f pull, Zou-He, collision, store
     if (owned) {
-      const float* pm = psi_row(0);
-      const float* pc = psi_row(1);
-      const float* pn = psi_row(2);
-      const int j = t + 1;
-      const float C = pC, E = pc[j + 1], Wv = pc[j - 1], N = pN, S = pS;
-      const float NE = pn[j + 1], NW = pn[j - 1], SE = pm[j + 1], SW = pm[j - 1];
-      const float gx = (4.0f * (E - Wv) + ((NE - NW) + (SE - SW))) * (1.0f / 12.0f);
-      const float gy = (4.0f * (N - S) + ((NE + NW) - (SE + SW))) * (1.0f / 12.0f);
-      const float lap = (4.0f * ((N + S) + (E + Wv)) + ((NE + NW) + (SE + SW)) - 20.0f * C) * (1.0f / 6.0f);
+      const DevStencil st = ring_stencil(ring, psi_row(0), psi_row(1), psi_row(2), t + 1, pS, pC, pN);
       const int rows[3] = {so[1], so[2], so[3]};
       const unsigned m = mask_at<SF, NT>(smem, rows[1] + L::OFF_M, t);
       float f[9];
@@ -452,12 +501,12 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
         const int o = (x == 0) ? 0 : 3;
         dev_zou_he_f(a.c, a.variant, a.H, a.W, x, y, f, (float)a.inlet_ux[y], a.side_in[(o + 0) * a.H + y],
                      a.side_in[(o + 1) * a.H + y], a.side_in[(o + 2) * a.H + y], drho_nb);
-        a.side_out[(o + 0) * a.H + y] = gx;
-        a.side_out[(o + 1) * a.H + y] = gy;
-        a.side_out[(o + 2) * a.H + y] = a.c.a * C * (1.0f - C * C) - a.c.kappa * lap;
+        a.side_out[(o + 0) * a.H + y] = st.gx;
+        a.side_out[(o + 1) * a.H + y] = st.gy;
+        a.side_out[(o + 2) * a.H + y] = dev_mu(a.c, st);
       }
       if (!(m & SOLID)) {
-        const DevMacro mc = dev_macros(a.c, f, C, gx, gy, lap);
+        const DevMacro mc = dev_macros(a.c, f, st);
         dev_collide(a.c, mc, f, gC);
       }
       const size_t q = (size_t)y * a.W + x;
@@ -550,7 +599,8 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
   using L = SlotLayout<SF, NT>;
   using M = TmaSmem<SF, NT, 4>;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
-  float* psi_ring = reinterpret_cast<float*>(smem + M::OFF_PSI);
+  const PsiRing<SF, NT, 4> ring(smem);
+  const float2 wallv = make_float2(a.c.psi_wall, 0.0f);
 
   const int t = threadIdx.x;
   const int x0 = band * NT;
@@ -563,7 +613,7 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
   const bool halo = (t == NT / 2) || (t == NT - 1);
 
   auto slot = [&](int r) { return M::OFF_SLOT + ((r - first) & 3) * M::SLOT; };
-  auto mrow = [&](int r) { return M::OFF_MASK + ((r - first) & 7) * L::RM; };
+  auto mrow = [&](int r) { return M::OFF_MASK + (int)((unsigned)(r - first) % (unsigned)M::MASK_ROWS) * L::RM; };
   // parity bits of the fills issued (thread 0), for the error path
   unsigned issued = phase;
   auto issue_g = [&](int r) {
@@ -590,19 +640,19 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
     for (int r = y0 - 1; r < y0 + 3; ++r) issue_f(r);
   }
   int pslot = 0;  // psi ring slot of row y0-1; rows y0-1, y0, y0+1 use pslot, +1, +2 (mod 4)
-  auto psi_row = [&](int k) { return psi_ring + ((pslot + k) & 3) * M::PSI_ROW; };
+  auto psi_row = [&](int k) { return ((pslot + k) & 3) * M::PSI_ROW; };
   // psi of ring row r (this thread's cell and its halo cell) into psi ring row k
   float gN[9];
   auto psi_of_row = [&](int r, int k) {
     const int rows[3] = {slot(r - 1), slot(r), slot(r + 1)};
     const bool ghost = walls && (r < 0 || r >= a.H);
     const int yr = wrap(r, a.H);
-    float* pr = psi_row(k);
-    const float pv = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(r), x, t, yr, gN);
-    pr[t + 1] = pv;
+    const int pr = psi_row(k);
+    const float2 pv = ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(r), x, t, yr, gN);
+    ring.put(pr, t + 1, pv);
     if (halo) {
       float gh[9];
-      pr[hl + 1] = ghost ? a.c.psi_wall : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(r), x0 + hl, hl, yr, gh);
+      ring.put(pr, hl + 1, ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(r), x0 + hl, hl, yr, gh));
     }
     return pv;
   };
@@ -612,11 +662,11 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
   wait_g(y0 - 2);
   wait_g(y0 - 1);
   wait_g(y0);
-  float pS = psi_of_row(y0 - 1, 0);  // psi of this column at rows y-1 and y
+  float2 pS = psi_of_row(y0 - 1, 0);  // psi of this column at rows y-1 and y
   __syncthreads();
   if (t == 0) issue_g(y0 + 2);
   wait_g(y0 + 1);
-  float pC = psi_of_row(y0, 1);
+  float2 pC = psi_of_row(y0, 1);
   float gC[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) gC[i] = gN[i];
@@ -628,7 +678,7 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
   for (int y = y0; y < y1; ++y) {
     // 1. psi of row y+1 from the g halves of rows y, y+1, y+2
     wait_g(y + 2);
-    const float pN = psi_of_row(y + 1, 2);
+    const float2 pN = psi_of_row(y + 1, 2);
     float drho_nb = 0.0f;
     if (walls && x == 0 && (y == 0 || y == a.H - 1)) drho_nb = inlet_corner_drho<SF, SCALED>(a, y == 0 ? 1 : a.H - 2);
     // 2. psi(y+1) complete: the g half of row y and the f half of row y-2 are
@@ -641,15 +691,7 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
     wait_f(y + 1);
     // 3. stencils, f pull, Zou-He, collision, store
     if (owned) {
-      const float* pm = psi_row(0);
-      const float* pc = psi_row(1);
-      const float* pn = psi_row(2);
-      const int j = t + 1;
-      const float C = pC, E = pc[j + 1], Wv = pc[j - 1], N = pN, S = pS;
-      const float NE = pn[j + 1], NW = pn[j - 1], SE = pm[j + 1], SW = pm[j - 1];
-      const float gx = (4.0f * (E - Wv) + ((NE - NW) + (SE - SW))) * (1.0f / 12.0f);
-      const float gy = (4.0f * (N - S) + ((NE + NW) - (SE + SW))) * (1.0f / 12.0f);
-      const float lap = (4.0f * ((N + S) + (E + Wv)) + ((NE + NW) + (SE + SW)) - 20.0f * C) * (1.0f / 6.0f);
+      const DevStencil st = ring_stencil(ring, psi_row(0), psi_row(1), psi_row(2), t + 1, pS, pC, pN);
       const int rows[3] = {slot(y - 1), slot(y), slot(y + 1)};
       const unsigned m = mask_at<SF, NT>(smem, mrow(y), t);
       float f[9];
@@ -658,12 +700,12 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
         const int o = (x == 0) ? 0 : 3;
         dev_zou_he_f(a.c, a.variant, a.H, a.W, x, y, f, (float)a.inlet_ux[y], a.side_in[(o + 0) * a.H + y],
                      a.side_in[(o + 1) * a.H + y], a.side_in[(o + 2) * a.H + y], drho_nb);
-        a.side_out[(o + 0) * a.H + y] = gx;
-        a.side_out[(o + 1) * a.H + y] = gy;
-        a.side_out[(o + 2) * a.H + y] = a.c.a * C * (1.0f - C * C) - a.c.kappa * lap;
+        a.side_out[(o + 0) * a.H + y] = st.gx;
+        a.side_out[(o + 1) * a.H + y] = st.gy;
+        a.side_out[(o + 2) * a.H + y] = dev_mu(a.c, st);
       }
       if (!(m & SOLID)) {
-        const DevMacro mc = dev_macros(a.c, f, C, gx, gy, lap);
+        const DevMacro mc = dev_macros(a.c, f, st);
         dev_collide(a.c, mc, f, gC);
       }
       const size_t q = (size_t)y * a.W + x;
@@ -734,6 +776,8 @@ constexpr int tma_resident_ctas() {
   const int n = 233472 / (TmaSmem<SF, NT, NS>::ALLOC + 256 + 1024);
   return n < 1 ? 1 : (n > 16 ? 16 : n);
 }
+static_assert(FD_TMA_NS_F32 != 4 || tma_resident_ctas<float, 128, 4>() >= 5,
+              "the FP32 split ring must fit five CTAs per SM");
 
 // CTA b takes band b % nbands of strip strip0 + b / nbands.  `tm`: the tensor
 // maps of the step's source planes (a grid constant: TMA reads it from the

@@ -3,12 +3,15 @@
 // fd_fused_step_packed needs two caller buffers for the Zou-He boundary
 // values (psi_x, psi_y, mu at columns 0 and W-1) because every iteration
 // reads the previous iteration's values and writes new ones.  Some callers
-// cannot provide the second one: a host that runs the step inside a CUDA
-// stream capture where a new allocation would be illegal, or a host whose
-// memory manager owns all device memory and does not let a library call
-// cudaMalloc behind its back.  For them, fd_fused_step_packed_noalloc keeps
-// the second boundary buffer in a fixed array in device memory that belongs
-// to this library, so the caller passes only its own state buffers.
+// cannot provide the second one: a host whose memory manager owns all of
+// device memory (a framework's caching allocator, or an arena reserved at
+// start-up) and does not let a library call cudaMalloc behind its back, or a
+// host that allocates everything once before it starts stepping.  For them,
+// fd_fused_step_packed_noalloc keeps the second boundary buffer in a fixed
+// array in device memory that belongs to this library, so the caller passes
+// only its own state buffers.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "fd_host.h"
@@ -27,26 +30,54 @@ constexpr int kNoAllocMaxH = 16384;
 static_assert(sizeof(g_noalloc_side) == sizeof(float) * 6 * kNoAllocMaxH, "buffer size");
 constexpr int kMaxDevices = 64;
 
-std::mutex g_setup_mutex;
-float* g_side_ptr[kMaxDevices] = {};
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
 
-// Device address of g_noalloc_side on the current device, looked up once
-// per device (the host-side name is only a stand-in for the symbol).
+// cuCtxGetCurrent from the driver through the runtime's entry-point query (the
+// library does not link libcuda); null if the driver does not offer it.
+CtxGetCurrentFn ctx_get_current_fn() {
+  static const CtxGetCurrentFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (CtxGetCurrentFn) nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
+
+std::mutex g_setup_mutex;
+struct SideScratch {
+  CUcontext ctx;
+  float* ptr;
+};
+SideScratch g_side[kMaxDevices] = {};
+
+// Device address of g_noalloc_side on the current device.  The host-side name
+// is only a stand-in for the symbol, so the address is looked up with
+// cudaGetSymbolAddress, once per device and context: a context torn down and
+// created again (cudaDeviceReset) is looked up afresh.
 int side_scratch(float** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return check_launch("fd_fused_step_packed_noalloc");
   FD_REQUIRE(dev >= 0 && dev < kMaxDevices, FD_ERR_ARG, "fd_fused_step_packed_noalloc: device %d out of range", dev);
+  const CtxGetCurrentFn get_ctx = ctx_get_current_fn();
+  FD_REQUIRE(get_ctx != nullptr, FD_ERR_CUDA, "fd_fused_step_packed_noalloc: cuCtxGetCurrent is not available");
+  CUcontext ctx = nullptr;  // null until the runtime has made the device's context current on this thread
+  if (get_ctx(&ctx) != CUDA_SUCCESS) ctx = nullptr;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (g_side_ptr[dev] == nullptr) {
+  if (ctx == nullptr || g_side[dev].ptr == nullptr || g_side[dev].ctx != ctx) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_side);
     if (e != cudaSuccess) {
       set_error("fd_fused_step_packed_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
       return FD_ERR_CUDA;
     }
-    g_side_ptr[dev] = static_cast<float*>(p);
+    FD_REQUIRE(get_ctx(&ctx) == CUDA_SUCCESS && ctx != nullptr, FD_ERR_CUDA,
+               "fd_fused_step_packed_noalloc: no current CUDA context");
+    g_side[dev] = SideScratch{ctx, static_cast<float*>(p)};
   }
-  *out = g_side_ptr[dev];
+  *out = g_side[dev].ptr;
   return FD_OK;
 }
 

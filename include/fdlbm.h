@@ -249,18 +249,24 @@ int fd_fused_step_packed(const fd_params* prm, const fd_storage* st, const uint1
                          void* pop_a, void* pop_b, void* side_a, void* side_b, int nsteps, int rows_per_warp,
                          void* stream);
 
-/* fd_fused_step_packed for callers that cannot allocate device memory (a
- * host that steps inside a CUDA stream capture, or one whose memory manager
- * owns all device memory).  The caller passes its state only: pop_a / pop_b as
- * in fd_fused_step_packed and ONE boundary buffer `side` (6*H floats, the
- * state's boundary values on entry and on return).  The second boundary
- * buffer is a fixed 384 KiB array inside this library (6 x 16384 floats), held
- * on every GPU that loads the library until the process exits; H > 16384 is
- * rejected with FD_ERR_SCRATCH.  The first call on a device looks up that
- * array's device address (make it before any stream capture).  All calls
- * share the array, so calls that overlap on the GPU (other streams, other host
- * threads) race; nothing in it needs clearing, every iteration writes all of
- * it before it is read.  No counterpart in the reference. */
+/* fd_fused_step_packed for callers that cannot allocate device memory: a
+ * host whose memory manager owns all of device memory (a framework's caching
+ * allocator, or an arena reserved at start-up) and does not let a library call
+ * cudaMalloc behind its back.  The caller passes its state only: pop_a / pop_b
+ * as in fd_fused_step_packed and ONE boundary buffer `side` (6*H floats, the
+ * state's boundary values on entry and on return).  The second boundary buffer
+ * is a fixed 384 KiB array inside this library (6 x 16384 floats), held on
+ * every GPU that loads the library until the process exits; H > 16384 is
+ * rejected with FD_ERR_SCRATCH.  The call allocates nothing (no cudaMalloc, no
+ * cudaFree, no allocating library routine).  Set-up on the first call on a
+ * device (and again after the device's context was torn down and created
+ * anew): the array's device address is looked up; the first call with a given
+ * storage type and rounding also raises the chosen kernel's shared-memory
+ * limit, as fd_fused_step_packed does, so make that first call before any
+ * stream capture.  All calls share the array, so calls that overlap on the GPU
+ * (other streams, other host threads) race; nothing in it needs clearing,
+ * every iteration writes all of it before it is read.  No counterpart in the
+ * reference. */
 int fd_fused_step_packed_noalloc(const fd_params* prm, const fd_storage* st, const uint16_t* mask,
                                  const double* inlet_ux, void* pop_a, void* pop_b, void* side, int nsteps,
                                  int rows_per_warp, void* stream);

@@ -102,16 +102,14 @@ def test_new_entry_points_check_their_arguments_on_the_host(lib):
 
 
 def test_integration_stub_struct_matches_the_binding():
-    """The ctypes stub shown to maintainers in INTEGRATION.md declares
-    fd_params with the same fields, types and size as the package binding."""
+    """The ctypes binding offered to the reference's maintainers
+    (fingering_dynamics_gb300/binding/reference_gb300.py, quoted in the
+    integration notes) declares fd_params and fd_storage with the same fields,
+    types and sizes as the package binding."""
     from fingering_dynamics_gb300 import _lib as L
-    text = open(os.path.join(REPO, "INTEGRATION.md")).read()
-    i = text.index("class fd_params(C.Structure):")
-    j = text.index("]", text.index("_fields_", i))
-    stub = re.findall(r'\("(\w+)", C\.(\w+)\)', text[i:j + 1])
-    assert [n for n, _ in stub] == [n for n, _ in L.fd_params._fields_]
-    fields = [(n, getattr(ctypes, t)) for n, t in stub]
-    Stub = type("Stub", (ctypes.Structure,), {"_fields_": fields})
-    assert ctypes.sizeof(Stub) == ctypes.sizeof(L.fd_params)
-    for (n, t), (_, u) in zip(fields, L.fd_params._fields_):
-        assert ctypes.sizeof(t) == ctypes.sizeof(u), n
+    from fingering_dynamics_gb300.binding import reference_gb300 as rb
+    for stub, ours in ((rb.fd_params, L.fd_params), (rb.fd_storage, L.fd_storage)):
+        assert [n for n, _ in stub._fields_] == [n for n, _ in ours._fields_]
+        assert ctypes.sizeof(stub) == ctypes.sizeof(ours)
+        for (n, t), (_, u) in zip(stub._fields_, ours._fields_):
+            assert ctypes.sizeof(t) == ctypes.sizeof(u), n

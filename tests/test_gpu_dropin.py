@@ -74,3 +74,29 @@ def test_reference_loop_on_dropin_is_bitwise(name):
     assert np.array_equal(cm.psi.cpu().numpy(), fx["s40_psi"])
     for k in ("rho", "ux", "uy", "p", "mu", "mix_tau"):
         assert np.array_equal(getattr(cm, k).cpu().numpy(), fx[f"s40_{k}"][mask]), k
+
+
+def test_reference_binding_stub_equals_the_fused_step():
+    """The ctypes binding offered to the reference's maintainers
+    (fingering_dynamics_gb300/binding/reference_gb300.py) run from a walled
+    module's globals gives, bit for bit, the package's own FP64 fused state."""
+    import types
+
+    from fingering_dynamics_gb300 import build
+    from fingering_dynamics_gb300 import geometry as geo
+    from fingering_dynamics_gb300.binding import reference_gb300 as rb
+    from fingering_dynamics_gb300.lattice import Lattice
+    from fingering_dynamics_gb300.params import walls_reference_params
+    lib = rb.load(build.build())
+    H, W, n = 32, 64, 7
+    prm = walls_reference_params().with_size(H, W)
+    g = geo.build_geometry(H, W, rects=[((20, 10), (26, 16))], walls=True)
+    mod = types.SimpleNamespace(__name__="fingering", H=H, W=W, tau=prm.tau, Eta_n=prm.eta_n, M=prm.M, a=prm.a,
+                                kappa=prm.kappa, gamma=prm.gamma, psi_wall=prm.psi_wall, u0=float(prm.inlet_ux[0]))
+    assert np.all(prm.inlet_ux == mod.u0)
+    got = rb.run(lib, mod, g.mask_word, prm.initial_psi(g.solid), n)
+    lat = Lattice(prm, g, dtype="f64")
+    lat.enter_fused()
+    lat.advance(n)
+    torch.cuda.synchronize()
+    assert torch.equal(got, lat.pop[lat.cur])

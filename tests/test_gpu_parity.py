@@ -3,9 +3,11 @@
 FP64: the reference-order kernels and the fused kernel are compared with the
 reference's own outputs bit for bit (the kernels keep the reference's
 operand order and are built without FMA contraction).
-FP32: per-colour densities after 500 steps agree with the reference's FP64
-run to 1e-5 relative (normwise: max |a - b| <= 1e-5 * max |b| per field),
-velocities to 2e-5 (see test_fused_500_steps_fp32_vs_reference).
+FP32: after 500 steps every fluid cell's rho_r = rho (1 + psi) / 2,
+rho_b = rho (1 - psi) / 2, u_x and u_y agree with the FP64 run (the
+reference's own, or the oracle's) to 1e-5 relative, cell by cell:
+|a - b| <= 1e-5 * max(|b|, floor), with the floor of each field given by
+percell_errors below.
 """
 import numpy as np
 import pytest
@@ -117,9 +119,37 @@ def _colour_fields(st):
     return {"rho_r": rho * (1 + psi) / 2, "rho_b": rho * (1 - psi) / 2, "ux": st["ux"], "uy": st["uy"]}
 
 
+# Floor of the per-cell relative bound.  rho_r and rho_b: 0.5, half the rest
+# density.  rho_r = rho (1 + psi) / 2 goes to 0 in the pure defending phase
+# (and rho_b in the invading one) while its difference stays at the absolute
+# difference of psi times rho / 2, so a bound relative to the cell's own
+# value alone would ask for a vanishing absolute error there.  u_x, u_y: the
+# run's inlet speed u0, the velocity scale the boundary imposes; in stagnant
+# cells (u -> 0) the bound is 1e-5 u0.
+RHO_FLOOR = 0.5
+
+
+def percell_errors(got_st, ref_st, u0):
+    """max over fluid cells of |a - b| / max(|b|, floor) per colour field."""
+    got, ref = _colour_fields(got_st), _colour_fields(ref_st)
+    out = {}
+    for k in got:
+        m = np.isfinite(ref[k])
+        assert np.isfinite(got[k][m]).all(), k
+        floor = u0 if k in ("ux", "uy") else RHO_FLOOR
+        out[k] = float((np.abs(got[k][m] - ref[k][m]) / np.maximum(np.abs(ref[k][m]), floor)).max())
+    return out
+
+
+def _fixture_state(fx, n=500):
+    return {k: fx[f"s{n}_{k}"] for k in ("rho", "psi", "ux", "uy")}
+
+
 def _rel_errors(st, fx, n=500):
+    """Normwise max |a - b| / max |b| per colour field (the looser measure the
+    reduced-precision and reference-order tests use)."""
     got = _colour_fields(st)
-    ref = _colour_fields({k: fx[f"s{n}_{k}"] for k in ("rho", "psi", "ux", "uy")})
+    ref = _colour_fields(_fixture_state(fx, n))
     out = {}
     for k in got:
         m = np.isfinite(ref[k])
@@ -127,23 +157,43 @@ def _rel_errors(st, fx, n=500):
     return out
 
 
-FP32_U_REL = 2e-5
-
-
 @pytest.mark.parametrize("name", LONG)
 def test_fused_500_steps_fp32_vs_reference(name):
-    """FP32 (deviation form, FP32 storage): rho_r, rho_b within 1e-5 relative
-    (max |a - b| / max |b| per field) of the reference's FP64 run, u within
-    2e-5.  The velocity difference (~1e-7 absolute) is set during the
-    start-up transient, when |u| reaches ~0.26 near the inlet, and does not
-    grow afterwards; the periodic case ends with max |u| = 0.0095, which
-    puts it at 1.25e-5 of the final field."""
+    """FP32 (deviation form, FP32 storage) after 500 steps against the
+    reference's own FP64 run, cell by cell: rho_r, rho_b, u_x, u_y within
+    1e-5 of max(|reference value|, floor) (percell_errors)."""
     fx = load(name)
     lat = make_lattice(fx, "f32")
     lat.step(500)
-    err = _rel_errors(lat.state(), fx)
-    assert err["rho_r"] <= FP32_REL and err["rho_b"] <= FP32_REL, err
-    assert err["ux"] <= FP32_U_REL and err["uy"] <= FP32_U_REL, err
+    err = percell_errors(lat.state(), _fixture_state(fx), float(fx["u0"]))
+    print(name, err)
+    assert all(e <= FP32_REL for e in err.values()), err
+
+
+def test_fused_500_steps_fp32_bench_generator_512x256():
+    """The 4096 x 2048 walls workload's generator (seeded circles and squares
+    to porosity 0.7, plug inlet u0 = 0.01, tau_inv 0.6 / tau_def 1.0,
+    interfacial tension 5e-4, 120 deg walls) rerun at 512 x 256: 500 packed
+    FP32 steps against the oracle's FP64 run of the same seeded input, cell by
+    cell within 1e-5 (percell_errors)."""
+    from bench import workload
+    from fingering_dynamics_gb300.lattice import Lattice
+    from oracle.lbm_oracle import OracleParams, OracleState
+    prm, g = workload(256, 512)
+    lat = Lattice(prm, g, dtype="f32")
+    lat.step(500)
+    got = lat.state()
+    op = OracleParams(H=prm.H, W=prm.W, variant="walls", tau=prm.tau, eta_n=prm.eta_n, M=prm.M, a=prm.a,
+                      kappa=prm.kappa, gamma=prm.gamma, psi_wall=prm.psi_wall, inlet_ux=prm.inlet_ux,
+                      outlet_coef=prm.outlet_coef)
+    st = OracleState(op, g.solid, prm.initial_psi(g.solid), init_mu=True, init_uy=True)
+    for _ in range(500):
+        st.step(g.corner_list, g.circle_masks)
+    ref = {"rho": st.full("rho"), "psi": np.where(g.solid, np.nan, st.psi), "ux": st.full("ux"), "uy": st.full("uy")}
+    assert all(np.isfinite(v[~g.solid]).all() for v in ref.values())
+    err = percell_errors(got, ref, float(prm.u0))
+    print("512x256", err)
+    assert all(e <= FP32_REL for e in err.values()), err
 
 
 def test_packed_register_kernel_w_not_multiple_of_8():
@@ -336,25 +386,32 @@ def test_pack_unpack_round_trip(dtype):
 
 
 def test_fused_matches_oracle_on_random_blocks():
-    """A geometry not in the fixtures: seeded circles and squares, walls."""
+    """A geometry not in the fixtures: seeded circles and squares, walls, with
+    the walls workload's parameters (tau_inv 0.6, plug inlet 0.01, 120 deg) at
+    48 x 96, on which the FP64 run stays finite.  After 300 fused FP64 steps
+    every field is finite in the oracle and the GPU equals it bit for bit."""
+    from bench import workload
     from fingering_dynamics_gb300 import geometry as geo
     from fingering_dynamics_gb300.lattice import Lattice
-    from fingering_dynamics_gb300.params import walls_reference_params
     from oracle.lbm_oracle import OracleParams, OracleState
     H, W = 48, 96
-    prm = walls_reference_params().with_size(H, W)
+    prm, _ = workload(H, W)
     rects, circles = geo.random_blocks(H, W, 0.8, 3, 6, seed=11, x_margin=8)
+    assert rects and circles
     g = geo.build_geometry(H, W, rects=rects, circles=circles, walls=True)
-    rng = np.random.default_rng(2)
-    rho0 = 1.0 - 0.001 * rng.random((H, W))
-    lat = Lattice(prm, g, dtype="f64", rho0=rho0)
-    lat.step(60)
+    lat = Lattice(prm, g, dtype="f64")
+    lat.step(300)
     op = OracleParams(H=H, W=W, variant="walls", tau=prm.tau, eta_n=prm.eta_n, M=prm.M, a=prm.a, kappa=prm.kappa,
                       gamma=prm.gamma, psi_wall=prm.psi_wall, inlet_ux=prm.inlet_ux, outlet_coef=prm.outlet_coef)
-    st = OracleState(op, g.solid, prm.initial_psi(g.solid), rho0=rho0, init_mu=True, init_uy=True)
-    for _ in range(60):
+    st = OracleState(op, g.solid, prm.initial_psi(g.solid), init_mu=True, init_uy=True)
+    for _ in range(300):
         st.step(g.corner_list, g.circle_masks)
     ref = oracle_fields(st)
+    for k in ("f", "g", "psi", "npx", "npy", "np2"):
+        assert np.isfinite(ref[k]).all(), k
+    for k in ("rho", "ux", "uy", "p", "mu", "mix_tau"):
+        assert np.isfinite(ref[k][~g.solid]).all(), k
     got = lat.state()
     for k in ("f", "g") + FIELDS:
-        assert _eq(got[k], ref[k]), (k, _first_diff(got[k], ref[k]))
+        assert np.array_equal(got[k], ref[k], equal_nan=k in ("rho", "ux", "uy", "p", "mu", "mix_tau")), \
+            (k, _first_diff(got[k], ref[k]))

@@ -2,7 +2,7 @@
 (tma_strip_split in fingering_dynamics_gb300/csrc/fd_fused_tma.cuh), no GPU.
 
 The kernel keeps four slots; the g half of ring row r (g_0, the g_i planes
-and the mask row, the mask into an 8-row mask ring) and its f half complete
+and the mask row, the mask into a 6-row mask ring) and its f half complete
 on separate mbarriers (0..3 g, 4..7 f).  The model replays, in program order,
 the prologue and the per-row loop: fills issued by the copy thread after each
 CTA barrier, waits with the parity bit of the next fill, and every read of a
@@ -15,7 +15,10 @@ is waited for before the strip ends.
 import pytest
 
 
-def run_strips(strips, mistake=None):
+MASK_ROWS = 6  # TmaSmem<float, NT, 4>::MASK_ROWS
+
+
+def run_strips(strips, mistake=None, mask_rows=MASK_ROWS):
     phase = 0
     fills = {b: [] for b in range(8)}
     waited = {b: 0 for b in range(8)}
@@ -29,7 +32,7 @@ def run_strips(strips, mistake=None):
             b = (r - first) & 3
             fills[b].append(("g", r))
             g_slot[b] = r
-            m_row[(r - first) & 7] = r
+            m_row[(r - first) % mask_rows] = r
 
         def issue_f(r):
             if r > y1:
@@ -60,7 +63,7 @@ def run_strips(strips, mistake=None):
             assert f_slot[(r - first) & 3] == r and r in done_f, ("f", r)
 
         def read_mask(r):
-            assert m_row[(r - first) & 7] == r and r in done_g, ("mask", r)
+            assert m_row[(r - first) % mask_rows] == r and r in done_g, ("mask", r)
 
         def psi_of(r):  # psi of row r: g of rows r-1 .. r+1, mask of row r
             for k in (r - 1, r, r + 1):
@@ -103,12 +106,15 @@ def test_split_ring_schedule(H):
         run_strips(strips[::-1] + strips)  # a persistent CTA taking several strips in a row
 
 
-@pytest.mark.parametrize("mistake", ["f_wait_after_the_pull", "g_fill_one_row_early", "f_fill_one_row_early"])
+@pytest.mark.parametrize("mistake", ["f_wait_after_the_pull", "g_fill_one_row_early", "f_fill_one_row_early",
+                                     "mask_ring_of_4_rows"])
 def test_model_catches_planted_mistakes(mistake):
     """The model is not vacuous: each schedule mistake planted in it (a wait
     moved after the reads it guards, a fill issued one row early into a slot
-    still being read) fails on some strip."""
+    still being read, a mask ring too short for the rows in flight) fails on
+    some strip."""
+    rows = 4 if mistake == "mask_ring_of_4_rows" else MASK_ROWS
     with pytest.raises((AssertionError, KeyError, IndexError)):
         for H in (8, 16, 33):
             for R in range(1, H + 1):
-                run_strips([(y0, min(y0 + R, H)) for y0 in range(0, H, R)], mistake)
+                run_strips([(y0, min(y0 + R, H)) for y0 in range(0, H, R)], mistake, mask_rows=rows)

@@ -2,10 +2,12 @@
 (fd_fused_step_packed_noalloc) against the regular one.
 
 It exists for callers that cannot allocate device memory themselves: a host
-stepping inside a CUDA stream capture, or one whose memory manager owns all
-of device memory.  Such a caller passes one boundary buffer instead of two; the
+whose memory manager owns all of device memory and does not let a library
+call cudaMalloc.  Such a caller passes one boundary buffer instead of two; the
 library keeps the second in a fixed device array.  Two calls in a row must give
-exactly what fd_fused_step_packed gives with two caller buffers.
+exactly what fd_fused_step_packed gives with two caller buffers, on both
+kernels the packed step uses (the staged kernel for widths that are a
+multiple of 8, the register kernel otherwise) and for FP32 and FP16 storage.
 """
 import ctypes as C
 
@@ -16,16 +18,16 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def _lattice():
+def _lattice(dtype, W):
     from fingering_dynamics_gb300 import build
     from fingering_dynamics_gb300 import geometry as geo
     from fingering_dynamics_gb300.lattice import Lattice
     from fingering_dynamics_gb300.params import walls_reference_params
     build.build()
-    H, W = 48, 96
+    H = 48
     prm = walls_reference_params().with_size(H, W)
     g = geo.build_geometry(H, W, rects=[((30, 12), (38, 20))], circles=[((64, 30), 6)], walls=True)
-    lat = Lattice(prm, g, dtype="f32")
+    lat = Lattice(prm, g, dtype=dtype)
     lat.enter_fused()
     return lat
 
@@ -34,13 +36,15 @@ def _p(t):
     return C.c_void_p(t.data_ptr())
 
 
+@pytest.mark.parametrize("W", [96, 92], ids=["staged_kernel", "register_kernel"])
+@pytest.mark.parametrize("dtype", ["f32", "f16"])
 @pytest.mark.parametrize("nsteps", [3, 4])
-def test_noalloc_matches_regular_entry_point(nsteps):
+def test_noalloc_matches_regular_entry_point(nsteps, dtype, W):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     from fingering_dynamics_gb300 import _lib as L
-    ref = _lattice()
-    lat = _lattice()
+    ref = _lattice(dtype, W)
+    lat = _lattice(dtype, W)
     a = [ref.ppop[ref.pcur].clone(), ref.ppop[1 - ref.pcur].clone()]
     b = [lat.ppop[lat.pcur].clone(), lat.ppop[1 - lat.pcur].clone()]
     sides = [ref.side[ref.scur].clone(), torch.zeros_like(ref.side[0])]
@@ -64,7 +68,7 @@ def test_noalloc_rejects_tall_lattice():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     from fingering_dynamics_gb300 import _lib as L
-    lat = _lattice()
+    lat = _lattice("f32", 96)
     prm = L.fd_params.from_buffer_copy(lat.prm)
     prm.H = 16385
     with pytest.raises(L.FDError) as e:
