@@ -13,6 +13,8 @@ import ctypes as C
 
 import pytest
 
+from fixtures import packed_planes
+
 pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
@@ -60,7 +62,9 @@ def test_noalloc_matches_regular_entry_point(nsteps, dtype, W):
             b.reverse()
             sides.reverse()
         torch.cuda.synchronize()
-        assert torch.equal(a[0], b[0]), f"populations differ after call {call + 1}"
+        # the planes only: the padding that rounds each plane up to 256 bytes is never written
+        assert torch.equal(packed_planes(a[0], ref.H, ref.W, dtype), packed_planes(b[0], lat.H, lat.W, dtype)), \
+            f"populations differ after call {call + 1}"
         assert torch.equal(sides[0], side), f"boundary values differ after call {call + 1}"
 
 
