@@ -19,6 +19,13 @@ them again (fd_fused_step_packed_host: the two copy directions and the
 kernel pipelined over row chunks).  With --gpus N > 1 each rank runs its own instance (replicas,
 weak scaling, no collective on the data path).
 
+The K-step timed region is repeated until the repetitions cover 0.5 s (so the
+clock sampler sees the load) and the median repetition is reported.  The
+default FP32 line also carries, measured the same way in the same process,
+the rest of the metric: `f16` and `bf16` (FP16 / BF16 storage of the same
+workload, 76 B per lattice update) and `ensemble` (the batched ensemble of 96
+seeded lattices, autotuned tile shape, CUDA-graph replay).
+
 --impl reference times the CPU implementation of the same step (the numpy
 oracle, which restates the reference's numpy code operation for operation)
 on the host cores: one process per core, each on a 512 x 256 sample of the
@@ -231,6 +238,101 @@ def job_mlups(world: int, cells: int, steps: int, ms_total: float) -> float:
     return world * cells * steps / (ms_total / 1e3) / 1e6
 
 
+MIN_TIMED_S = 0.5  # the K-step timed region is repeated until the repetitions cover at least this long
+
+
+def timed_repetitions(run_steps, stream, min_s=MIN_TIMED_S, max_reps=5000, barrier=None):
+    """Milliseconds of each repetition of `run_steps()` (one timed region of K
+    steps, CUDA events on `stream`, synchronised and, with `barrier`, a barrier
+    over ranks on both sides), repeated until the repetitions cover `min_s`
+    seconds.  With several ranks every rank stops after the same repetition."""
+    import torch
+    out = []
+    total = 0.0
+    while len(out) < max_reps:
+        torch.cuda.synchronize()
+        if barrier is not None:
+            barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run_steps()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if barrier is not None:
+            barrier()
+        out.append(e0.elapsed_time(e1))
+        total += out[-1]
+        done = total >= min_s * 1e3
+        if barrier is not None:
+            done = max_over_ranks([float(done)], device=f"cuda:{torch.cuda.current_device()}")[0] > 0
+        if done:
+            break
+    return out
+
+
+def roofline(dtype, cells, ms_step):
+    alg_bytes = BYTES_PER_LU[dtype] * cells
+    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg_bytes}
+
+
+def measure_single(prm, g, dtype, steps, warmup, rows=0, rounding="stochastic"):
+    """A storage type on the single-lattice workload: `warmup` steps, then the
+    K-step timed region repeated (timed_repetitions); median ms per step."""
+    import torch
+    from fingering_dynamics_gb300.lattice import Lattice
+    lat = Lattice(prm, g, dtype=dtype, rounding=rounding)
+    lat.enter_fused()
+    lat.advance(warmup, rows)
+    stream = torch.cuda.current_stream()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        reps = timed_repetitions(lambda: lat.advance(steps, rows), stream)
+    ms_step = statistics.median(reps) / steps
+    lat.exit_fused()
+    finite = bool(torch.isfinite(lat.psi).all().item())
+    del lat
+    torch.cuda.empty_cache()
+    return {"dtype": dtype, "value": round(prm.H * prm.W / (ms_step / 1e3) / 1e6, 1), "unit": "MLUPS",
+            "ms_per_step": round(ms_step, 4), "timed_repetitions": len(reps), "steps_per_repetition": steps,
+            "roofline": roofline(dtype, prm.H * prm.W, ms_step),
+            "rounding": rounding if dtype in ("f16", "bf16") else None, "state_finite_after_timing": finite,
+            "gpu_launches_per_repetition": steps, "clocks": clk.summary()}
+
+
+def measure_ensemble(steps, warmup, members=96, dtype="f32", family="stable", seed=2024):
+    """The batched ensemble (seeded lattices of uneven size, geometry and
+    parameters; one persistent launch per iteration replayed from a CUDA graph;
+    tile shape autotuned on the ensemble): aggregate MLUPS, median over
+    repetitions of the K-step timed region."""
+    import torch
+    from fingering_dynamics_gb300.ensemble import Ensemble, ensemble_specs
+    specs = ensemble_specs(members, seed=seed, family=family)
+    ens = Ensemble([s.build() for s in specs], dtype=dtype)
+    tuned = ens.autotune(steps=10)
+    ens.step(warmup)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        reps = timed_repetitions(lambda: ens.step(steps, use_graph=True), ens.stream)
+    ms_step = statistics.median(reps) / steps
+    finite = []
+    for lat in ens.lattices:
+        d = lat.diagnostics()
+        finite.append(bool(np.isfinite(d["mass_r"]) and np.isfinite(d["mass_b"])))
+    out = {"dtype": dtype, "members": members, "family": family, "cells": ens.cells,
+           "value": round(ens.cells / (ms_step / 1e3) / 1e6, 1), "unit": "MLUPS", "ms_per_step": round(ms_step, 4),
+           "timed_repetitions": len(reps), "steps_per_repetition": steps,
+           "roofline": roofline(dtype, ens.cells, ms_step),
+           "tile_shape": {"band_width": ens.config[0], "rows_per_strip": ens.config[1]},
+           "autotune_mlups": {f"{b}x{r}": round(v, 1) for (b, r), v in tuned.items()},
+           "members_finite": int(sum(finite)), "graph": True, "gpu_launches_per_repetition": steps,
+           "clocks": clk.summary()}
+    ens.close()
+    del ens
+    torch.cuda.empty_cache()
+    return out
+
+
 # ---------------------------------------------------------------------------
 # GPU timing
 # ---------------------------------------------------------------------------
@@ -261,17 +363,14 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     torch.cuda.synchronize()
     barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # the K-step timed region (synchronize and barrier on both sides), repeated
+    # until the repetitions cover MIN_TIMED_S; the median repetition is reported
     with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
-        barrier()
-        e0.record(stream)
-        for _ in range(args.steps):
-            lat.advance(1, args.rows)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-    ms_total = e0.elapsed_time(e1)
+        def region():
+            for _ in range(args.steps):
+                lat.advance(1, args.rows)
+        reps = timed_repetitions(region, stream, barrier=barrier if world > 1 else None)
+    ms_total = statistics.median(reps)
     clocks = clk.summary()
     lat.exit_fused()
     finite = bool(torch.isfinite(lat.psi).all().item())
@@ -339,9 +438,19 @@ def run_ours(args):
                         f"pipelined host step, chunk rows {args.e2e_chunk_rows or 'auto'}"},
             "gpu_launches": args.steps,
             "clocks": clocks,
+            "timed_repetitions": {"count": len(reps), "steps_each": args.steps,
+                                  "ms_median": round(statistics.median(reps), 4), "ms_min": round(min(reps), 4),
+                                  "ms_max": round(max(reps), 4)},
             # fluid cells only (the metric counts every cell, solid ones too, as the reference streams them)
             "mflups_fluid": round(mlups * g.porosity, 1),
         }
+        if not args.no_extras and args.dtype == "f32" and world == 1:
+            # the rest of the metric on the same box and workload: reduced-precision storage and the batch
+            for d in ("f16", "bf16"):
+                sub = measure_single(prm, g, d, args.steps, args.warmup, args.rows, args.rounding)
+                sub["ratio_to_f32"] = round(sub["value"] / mlups, 3)
+                line[d] = sub
+            line["ensemble"] = measure_ensemble(args.steps, args.warmup)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
         print(json.dumps(line), flush=True)
@@ -595,6 +704,8 @@ def main():
     ap.add_argument("--rows", type=int, default=0, help="rows per warp (0 = automatic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end measurement")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="single workload: skip the f16 / bf16 and ensemble sub-records of the default line")
     ap.add_argument("--e2e-chunk-rows", type=int, default=0,
                     help="e2e: rows per chunk of the pipelined host step (0: automatic)")
     ap.add_argument("--e2e-serial", action="store_true",

@@ -10,7 +10,9 @@ import os
 import threading
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "_lib", "libfdlbm.so")
+# the in-tree build; FDLBM_LIBRARY names another build of the same sources (built with other
+# compile-time tile options: python -m fingering_dynamics_gb300.build --out DIR --define ...)
+LIB_PATH = os.environ.get("FDLBM_LIBRARY") or os.path.join(PKG, "_lib", "libfdlbm.so")
 
 FD_OK = 0
 FD_F64, FD_F32, FD_F16, FD_BF16 = 0, 1, 2, 3

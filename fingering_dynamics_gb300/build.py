@@ -5,7 +5,11 @@ reference-order units get ``-fmad=false`` (the reference's arithmetic
 without contraction), the others keep FMA contraction.  The shared library
 lands in ``fingering_dynamics_gb300/_lib/``.
 
-    python -m fingering_dynamics_gb300.build [--force] [--verbose]
+    python -m fingering_dynamics_gb300.build [--force] [--verbose] [--out DIR] [--define NAME=VALUE ...]
+
+--out / --define build another copy of the library with compile-time options
+(e.g. FD_TMA_NS_16=6) into DIR; point FDLBM_LIBRARY at DIR/libfdlbm.so to
+load it instead of the in-tree build.
 """
 from __future__ import annotations
 
@@ -62,39 +66,44 @@ def _sources_digest(extra: list[str]) -> str:
     return h.hexdigest()
 
 
-def _up_to_date(stamp: str, digest: str) -> bool:
-    if not (os.path.exists(LIB) and os.path.exists(stamp)):
+def _up_to_date(lib_path: str, stamp: str, digest: str) -> bool:
+    if not (os.path.exists(lib_path) and os.path.exists(stamp)):
         return False
     with open(stamp) as fh:
         return fh.read().strip() == digest
 
 
-def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False, out: str | None = None,
+          defines: tuple[str, ...] = ()) -> str:
     """Compile and link when the sources changed.  Concurrent callers (one per
     rank of a multi-GPU run) serialise on a lock file; the later ones find the
-    library already built."""
-    os.makedirs(OUT, exist_ok=True)
-    extra = ["-Xptxas", "-v"] if ptxas_info else []
+    library already built.  `out` / `defines`: another build directory and
+    extra -D options (see the module docstring)."""
+    out = os.path.abspath(out) if out else OUT
+    lib_path = os.path.join(out, "libfdlbm.so")
+    os.makedirs(out, exist_ok=True)
+    extra = (["-Xptxas", "-v"] if ptxas_info else []) + [f"-D{d}" for d in defines]
     digest = _sources_digest(extra)
-    stamp = os.path.join(OUT, "libfdlbm.sha256")
-    if not force and _up_to_date(stamp, digest):
-        return LIB
-    with open(os.path.join(OUT, ".build.lock"), "w") as lock:
+    stamp = os.path.join(out, "libfdlbm.sha256")
+    if not force and _up_to_date(lib_path, stamp, digest):
+        return lib_path
+    with open(os.path.join(out, ".build.lock"), "w") as lock:
         fcntl.flock(lock, fcntl.LOCK_EX)
         try:
-            if not force and _up_to_date(stamp, digest):
-                return LIB
-            return _compile_and_link(digest, stamp, extra, verbose)
+            if not force and _up_to_date(lib_path, stamp, digest):
+                return lib_path
+            return _compile_and_link(digest, stamp, extra, verbose, out)
         finally:
             fcntl.flock(lock, fcntl.LOCK_UN)
 
 
-def _compile_and_link(digest: str, stamp: str, extra: list, verbose: bool) -> str:
+def _compile_and_link(digest: str, stamp: str, extra: list, verbose: bool, out: str) -> str:
     cc = nvcc()
     objs = []
+    lib_path = os.path.join(out, "libfdlbm.so")
 
     def compile_one(name):
-        obj = os.path.join(OUT, name.replace(".cu", ".o"))
+        obj = os.path.join(out, name.replace(".cu", ".o"))
         cmd = [cc, *ARCH, *COMMON, *UNITS[name], *extra, "-c", os.path.join(CSRC, name), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -106,15 +115,15 @@ def _compile_and_link(digest: str, stamp: str, extra: list, verbose: bool) -> st
             objs.append(obj)
             if verbose and log.strip():
                 print(log, file=sys.stderr)
-    tmp = LIB + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib_path)
     with open(stamp, "w") as fh:
         fh.write(digest)
-    return LIB
+    return lib_path
 
 
 if __name__ == "__main__":
@@ -122,5 +131,8 @@ if __name__ == "__main__":
     ap.add_argument("--force", action="store_true")
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--ptxas-info", action="store_true")
+    ap.add_argument("--out", default=None, help="build directory (default: the in-tree fingering_dynamics_gb300/_lib)")
+    ap.add_argument("--define", action="append", default=[], help="extra preprocessor definition NAME=VALUE")
     a = ap.parse_args()
-    print(build(force=a.force, verbose=a.verbose or a.ptxas_info, ptxas_info=a.ptxas_info))
+    print(build(force=a.force, verbose=a.verbose or a.ptxas_info, ptxas_info=a.ptxas_info, out=a.out,
+                defines=tuple(a.define)))
