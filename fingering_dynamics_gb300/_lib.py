@@ -22,7 +22,10 @@ FD_ROUND_NEAREST, FD_ROUND_STOCHASTIC = 0, 1
 ROUNDING = {"nearest": FD_ROUND_NEAREST, "stochastic": FD_ROUND_STOCHASTIC}
 TERMS = {"large_F": 0, "feq": 1, "geq": 2, "F": 3, "G": 4}
 FIELDS = {"rho": 0, "npx": 1, "npy": 2, "np2": 3, "mu": 4, "mu_plain": 5, "ux": 6, "uy": 7, "p": 8, "mix_tau": 9, "psi": 10}
-ERRORS = {-1: "FD_ERR_ARG", -2: "FD_ERR_SHAPE", -3: "FD_ERR_CUDA", -4: "FD_ERR_DTYPE", -5: "FD_ERR_SCRATCH"}
+ERRORS = {-1: "FD_ERR_ARG", -2: "FD_ERR_SHAPE", -3: "FD_ERR_CUDA", -4: "FD_ERR_DTYPE", -5: "FD_ERR_SCRATCH",
+          -6: "FD_ERR_NONFINITE"}
+FD_ERR_NONFINITE = -6
+FD_STATUS_WAIT_TIMEOUT, FD_STATUS_NONFINITE = 1, 2
 
 
 class FDError(RuntimeError):
@@ -98,6 +101,7 @@ SIGNATURES = {
     "fd_batch_configure": [_VP, _I, _I],
     "fd_batch_step": [_VP, _I, _I, _VP],
     "fd_batch_parity": [_VP],
+    "fd_batch_member_status": [_VP, C.POINTER(C.c_uint32), _I],
     "fd_batch_tiles": [_VP],
     "fd_batch_grid": [_VP],
     "fd_batch_destroy": [_VP],

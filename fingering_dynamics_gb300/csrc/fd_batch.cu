@@ -23,13 +23,14 @@ struct fd_batch {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t graph_stream = nullptr;
   unsigned* d_ctl = nullptr;  // step and tile counters, two slots each (k_fused_tma_batch)
+  unsigned* d_status = nullptr;  // per member: nonzero once a non-finite cell was met (quarantined)
 };
 
 namespace fd {
 namespace {
 
 template <typename SF>
-DevArgs<SF> instance_args(const fd_instance& in, const fd_storage& st, int rows, bool swap) {
+DevArgs<SF> instance_args(const fd_instance& in, const fd_storage& st, int rows, bool swap, unsigned* status) {
   const fd_params& p = in.prm;
   const PackedLayout<SF> L = packed_layout<SF>(p.H, p.W);
   DevArgs<SF> a;
@@ -57,6 +58,7 @@ DevArgs<SF> instance_args(const fd_instance& in, const fd_storage& st, int rows,
   a.side_in = (const float*)(swap ? in.side_b : in.side_a);
   a.side_out = (float*)(swap ? in.side_a : in.side_b);
   a.seed = in.seed;  // hashed with the batch step counter in the kernel
+  a.status = status;
   return a;
 }
 
@@ -69,8 +71,8 @@ int prepare(fd_batch* b) {
   std::vector<BatchInst<SF>> hi(b->n);
   std::vector<int4> tiles;
   for (int i = 0; i < b->n; ++i) {
-    hi[i].args[0] = instance_args<SF>(b->inst[i], b->st, b->rows, false);
-    hi[i].args[1] = instance_args<SF>(b->inst[i], b->st, b->rows, true);
+    hi[i].args[0] = instance_args<SF>(b->inst[i], b->st, b->rows, false, b->d_status + i);
+    hi[i].args[1] = instance_args<SF>(b->inst[i], b->st, b->rows, true, b->d_status + i);
     if (int r = tma_maps<SF, NT>(hi[i].args[0], (const char*)b->inst[i].pop_a, hi[i].maps[0])) return r;
     if (int r = tma_maps<SF, NT>(hi[i].args[1], (const char*)b->inst[i].pop_b, hi[i].maps[1])) return r;
     const int nb = (b->inst[i].prm.W + NT - 1) / NT, ns = hi[i].args[0].nstrips;
@@ -200,7 +202,9 @@ int fd_batch_create(const fd_instance* inst, int n, const fd_storage* st, int ro
   b->rows = rows_per_strip;
   b->inst.assign(inst, inst + n);
   if (cudaMalloc(&b->d_ctl, 4 * sizeof(unsigned)) != cudaSuccess ||
-      cudaMemset(b->d_ctl, 0, 4 * sizeof(unsigned)) != cudaSuccess) {
+      cudaMemset(b->d_ctl, 0, 4 * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&b->d_status, (size_t)n * sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(b->d_status, 0, (size_t)n * sizeof(unsigned)) != cudaSuccess) {
     const int r = check_launch("fd_batch_create: step counter");
     fd_batch_destroy(b);
     return r;
@@ -257,6 +261,18 @@ int fd_batch_step(fd_batch* b, int nsteps, int use_graph, void* stream) {
 
 int fd_batch_parity(const fd_batch* b) { return b ? b->parity : -1; }
 
+int fd_batch_member_status(fd_batch* b, uint32_t* out, int clear) {
+  FD_REQUIRE(b != nullptr && out != nullptr, FD_ERR_ARG, "fd_batch_member_status: NULL pointer");
+  if (cudaDeviceSynchronize() != cudaSuccess ||
+      cudaMemcpy(out, b->d_status, (size_t)b->n * sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return check_launch("fd_batch_member_status");
+  if (clear && cudaMemset(b->d_status, 0, (size_t)b->n * sizeof(unsigned)) != cudaSuccess)
+    return check_launch("fd_batch_member_status: clear");
+  for (int i = 0; i < b->n; ++i)
+    FD_REQUIRE(out[i] == 0, FD_ERR_NONFINITE, "fd_batch_member_status: member %d met a non-finite cell", i);
+  return FD_OK;
+}
+
 int fd_batch_tiles(const fd_batch* b) { return b ? b->ntiles : -1; }
 
 int fd_batch_grid(const fd_batch* b) { return b ? b->grid : -1; }
@@ -267,6 +283,7 @@ int fd_batch_destroy(fd_batch* b) {
   cudaFree(b->d_inst);
   cudaFree(b->d_tiles);
   cudaFree(b->d_ctl);
+  cudaFree(b->d_status);
   delete b;
   return FD_OK;
 }
@@ -275,7 +292,7 @@ int fd_batch_destroy(fd_batch* b) {
 
 namespace fd {
 
-// This unit's copy of the device error word (fd_fused_tma.cuh), which the
+// This unit's copy of the device error word (fd_fused_dev.cuh), which the
 // batched kernel latches; fd_device_status() combines it with the others.
 int batch_device_error(unsigned* out, bool clear) { return device_error_word(out, clear); }
 

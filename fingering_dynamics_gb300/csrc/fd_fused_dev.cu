@@ -4,6 +4,9 @@
 #include "fd_host.h"
 
 namespace fd {
+// This unit's copy of the device status word (fd_fused_dev.cuh), which the
+// register kernel latches; fd_device_status() combines it with the others.
+int dev_device_error(unsigned* out, bool clear) { return device_error_word(out, clear); }
 int fused_tma(const fd_params& p, const fd_storage& st, const DevCoef& c, const uint16_t* mask,
               const double* inlet_ux, void* pa, void* pb, void* sa, void* sb, int nsteps, int R, cudaStream_t s);
 int tma_band_width();

@@ -24,6 +24,33 @@ constexpr int kDevLanes = 30;
 
 inline size_t plane_bytes(size_t P, size_t elem) { return (P * elem + 255) / 256 * 256; }
 
+// Device-side status word of the library's packed kernels:
+//   bit 0 (kStatusWaitTimeout)  a bounded wait on an asynchronous copy gave up;
+//   bit 1 (kStatusNonFinite)    a fused step met a non-finite density or psi in a
+//                               fluid cell (numpy raises FloatingPointError there
+//                               under the reference's np.seterr(all='raise'),
+//                               fingering_periodic.py:496).
+// The library is built without relocatable device code, so every translation
+// unit that includes this header has its own copy, read and cleared through
+// its own device_error_word(); fd_device_status() combines the copies.
+constexpr unsigned kStatusWaitTimeout = 1u;
+constexpr unsigned kStatusNonFinite = 2u;
+__device__ unsigned int g_fd_device_error = 0;
+
+namespace {
+inline int device_error_word(unsigned* out, bool clear) {
+  if (cudaMemcpyFromSymbol(out, g_fd_device_error, sizeof(unsigned)) != cudaSuccess) return FD_ERR_CUDA;
+  if (clear) {
+    const unsigned zero = 0;
+    if (cudaMemcpyToSymbol(g_fd_device_error, &zero, sizeof(unsigned)) != cudaSuccess) return FD_ERR_CUDA;
+  }
+  return FD_OK;
+}
+}  // namespace
+
+// true if rho or psi of a fluid cell is not finite (NaN or +-inf)
+__device__ __forceinline__ bool nonfinite_cell(float rho, float psi) { return !(fabsf(rho) + fabsf(psi) < INFINITY); }
+
 template <typename SF>
 struct DevArgs {
   DevCoef c;
@@ -40,7 +67,17 @@ struct DevArgs {
   const float* __restrict__ side_in;
   float* __restrict__ side_out;
   uint32_t seed;  // stochastic rounding: sr_hash of the step's seed
+  // where a non-finite cell is reported: a batch member's status word (set to
+  // 1; the batched kernel skips the member's tiles from then on), or null for
+  // the unit's device status word (bit kStatusNonFinite)
+  unsigned* status;
 };
+
+template <typename SF>
+__device__ __forceinline__ void report_nonfinite(const DevArgs<SF>& a) {
+  if (a.status) atomicOr(a.status, 1u);
+  else atomicOr(&g_fd_device_error, kStatusNonFinite);
+}
 
 template <typename S, int VEC>
 __device__ __forceinline__ void ld_conv(const S* __restrict__ p, float scale, float (&out)[VEC]) {
@@ -293,6 +330,7 @@ __global__ void __launch_bounds__(128, FD_DEV_MINB) k_fused_dev(const DevArgs<SF
   float gC[9][VEC], gN[9][VEC];
   float2 Pm[VEC], Pc[VEC], Pn[VEC];
   uint16_t mC[VEC], mN[VEC];
+  bool bad = false;  // a fluid cell with a non-finite rho or psi
 
   if (walls && y0 == 0) {
 #pragma unroll
@@ -336,6 +374,7 @@ __global__ void __launch_bounds__(128, FD_DEV_MINB) k_fused_dev(const DevArgs<SF
 #pragma unroll
         for (int i = 0; i < 9; ++i) { fc[i] = f[i][k]; gc[i] = gC[i][k]; }
         const DevMacro m = dev_macros(a.c, fc, st[k]);
+        bad |= nonfinite_cell(m.rho, m.psi);
         dev_collide(a.c, m, fc, gc);
 #pragma unroll
         for (int i = 0; i < 9; ++i) { f[i][k] = fc[i]; gC[i][k] = gc[i]; }
@@ -369,6 +408,7 @@ __global__ void __launch_bounds__(128, FD_DEV_MINB) k_fused_dev(const DevArgs<SF
       for (int i = 0; i < 9; ++i) gC[i][k] = gN[i][k];
     }
   }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) report_nonfinite(a);
 }
 
 // ---- pack / unpack between the reference layout (18 planes of T) and the
@@ -432,6 +472,7 @@ int launch_fused_dev(const fd_params& p, const DevCoef& c, const uint16_t* mask,
   a.pstride_f = L.pstride;
   a.mask = mask;
   a.inlet_ux = inlet_ux;
+  a.status = nullptr;
   const long long warps = (long long)a.nchunks * a.nstrips;
   const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
   for (int s = 0; s < nsteps; ++s) {

@@ -81,6 +81,7 @@ int fused_tma_strips(const fd_params& p, const fd_storage& st, const DevCoef& c,
 }
 
 int batch_device_error(unsigned* out, bool clear);
+int dev_device_error(unsigned* out, bool clear);
 int batch_selftest_wait_timeout(unsigned polls, cudaStream_t s);
 
 // One thread waits, through the staged kernel's bounded wait, on an mbarrier
@@ -109,9 +110,10 @@ extern "C" int fd_selftest_wait_timeout(unsigned polls, int unit, void* stream) 
 
 extern "C" int fd_device_status(unsigned* out, int clear) {
   FD_REQUIRE(out != nullptr, FD_ERR_ARG, "fd_device_status: NULL pointer");
-  unsigned single = 0, batch = 0;
-  if (fd::device_error_word(&single, clear != 0) != FD_OK || fd::batch_device_error(&batch, clear != 0) != FD_OK)
+  unsigned single = 0, batch = 0, reg = 0;
+  if (fd::device_error_word(&single, clear != 0) != FD_OK || fd::batch_device_error(&batch, clear != 0) != FD_OK ||
+      fd::dev_device_error(&reg, clear != 0) != FD_OK)
     return fd::check_launch("fd_device_status");
-  *out = single | batch;
+  *out = single | batch | reg;
   return FD_OK;
 }

@@ -64,24 +64,6 @@ constexpr bool psi_paired() {
 constexpr float kPsiLoScale = 16777216.0f;          // 2^24
 constexpr float kPsiLoInv = 1.0f / 16777216.0f;
 
-// Device-side error word: bit 0 = an mbarrier wait gave up (copy never
-// completed).  The library is built without relocatable device code, so every
-// translation unit that includes this header has its own copy, read and
-// cleared through its own device_error_word(); fd_device_status() combines
-// the copies of all units.
-__device__ unsigned int g_fd_device_error = 0;
-
-namespace {
-inline int device_error_word(unsigned* out, bool clear) {
-  if (cudaMemcpyFromSymbol(out, g_fd_device_error, sizeof(unsigned)) != cudaSuccess) return FD_ERR_CUDA;
-  if (clear) {
-    const unsigned zero = 0;
-    if (cudaMemcpyToSymbol(g_fd_device_error, &zero, sizeof(unsigned)) != cudaSuccess) return FD_ERR_CUDA;
-  }
-  return FD_OK;
-}
-}  // namespace
-
 constexpr unsigned kWaitLimit = 1u << 24;  // bounded spins on an mbarrier
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -124,7 +106,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsign
         : "memory");
     if (done) return true;
   }
-  atomicOr(&g_fd_device_error, 1u);
+  atomicOr(&g_fd_device_error, kStatusWaitTimeout);
   return false;
 }
 
@@ -434,6 +416,7 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
 
   float gC[9], gN[9];
   float2 pS = wallv, pC = wallv;  // psi of this column at rows y-1 and y
+  bool bad = false;               // a fluid cell with a non-finite rho or psi
   // prologue: psi of rows y0-1 and y0 (needs rows y0-2 .. y0+1)
   wait_slot(0);
   wait_slot(1);
@@ -507,6 +490,7 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
       }
       if (!(m & SOLID)) {
         const DevMacro mc = dev_macros(a.c, f, st);
+        bad |= nonfinite_cell(mc.rho, mc.psi);
         dev_collide(a.c, mc, f, gC);
       }
       const size_t q = (size_t)y * a.W + x;
@@ -558,6 +542,7 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
       mbar_wait(&bars[s], (unsigned)((k / NS) & 1));
     }
   }
+  if (__syncthreads_or(bad) && t == 0) report_nonfinite(a);
   ok = __syncthreads_and(ok);
 }
 
@@ -663,6 +648,7 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
   wait_g(y0 - 1);
   wait_g(y0);
   float2 pS = psi_of_row(y0 - 1, 0);  // psi of this column at rows y-1 and y
+  bool bad = false;                   // a fluid cell with a non-finite rho or psi
   __syncthreads();
   if (t == 0) issue_g(y0 + 2);
   wait_g(y0 + 1);
@@ -706,6 +692,7 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
       }
       if (!(m & SOLID)) {
         const DevMacro mc = dev_macros(a.c, f, st);
+        bad |= nonfinite_cell(mc.rho, mc.psi);
         dev_collide(a.c, mc, f, gC);
       }
       const size_t q = (size_t)y * a.W + x;
@@ -744,6 +731,7 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
   if (!ok && t == 0) {
     for (int b = 0; b < M::NBAR; ++b) mbar_wait(&bars[b], ((issued >> b) & 1u) ^ 1u);
   }
+  if (__syncthreads_or(bad) && t == 0) report_nonfinite(a);
   ok = __syncthreads_and(ok);
 }
 
@@ -823,6 +811,7 @@ __global__ void __launch_bounds__(NT, (NS == 4 ? tma_resident_ctas<SF, NT, NS>()
   __shared__ DevArgs<SF> sa;
   __shared__ const TmaMaps* stm;
   __shared__ int next;
+  __shared__ int skip;
   char* smem = smem_aligned(smem_raw);
   init_ring<SF, NT, NS>(smem);
   unsigned done = 0;
@@ -836,15 +825,22 @@ __global__ void __launch_bounds__(NT, (NS == 4 ? tma_resident_ctas<SF, NT, NS>()
   for (;;) {
     if (threadIdx.x == 0) {
       next = (int)atomicAdd(&ctl[2 + parity], 1u);
+      skip = 0;
       if (next < ntiles) {
         sa = inst[tiles[next].x].args[parity];
         stm = &inst[tiles[next].x].maps[parity];
         if constexpr (STOCH) sa.seed = sr_hash(sa.seed + done);
+        // a quarantined member (non-finite cell seen) is not stepped any more
+        skip = *reinterpret_cast<volatile unsigned*>(sa.status) != 0u;
       }
     }
     __syncthreads();
     const int k = next;
     if (k >= ntiles || !ok) break;
+    if (skip) {
+      __syncthreads();  // every thread has read next / skip before thread 0 rewrites them
+      continue;
+    }
     const int4 tl = tiles[k];
     tma_strip<SF, NT, NS, SCALED, STOCH>(sa, stm, tl.y, tl.z, smem, phase, ok);
   }
@@ -897,6 +893,7 @@ DevArgs<SF> tma_args(const fd_params& p, const DevCoef& c, const uint16_t* mask,
   a.pstride_f = L.pstride;
   a.mask = mask;
   a.inlet_ux = inlet_ux;
+  a.status = nullptr;
   const int nbands = (p.W + NT - 1) / NT;
   if (R <= 0) {
     int per_sm = 1;

@@ -246,6 +246,18 @@ class Ensemble:
     def diagnostics(self) -> list[dict]:
         return [lat.diagnostics() for lat in self.lattices]
 
+    def member_status(self, clear: bool = False) -> list[bool]:
+        """True for every member that met a non-finite density or psi and is
+        quarantined: the batch skips its tiles from then on while the others
+        keep stepping (include/fdlbm.h fd_batch_member_status).  ``clear``
+        releases every member afterwards (restore their states first)."""
+        n = len(self.lattices)
+        out = (C.c_uint32 * n)()
+        r = L.lib().fd_batch_member_status(self._batch, out, int(bool(clear)))
+        if r not in (L.FD_OK, L.FD_ERR_NONFINITE):
+            raise L.FDError(r, "fd_batch_member_status", L.lib().fd_last_error().decode(errors="replace"))
+        return [bool(v) for v in out]
+
     def close(self):
         if self._batch:
             L.lib().fd_batch_destroy(self._batch)

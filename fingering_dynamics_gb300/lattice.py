@@ -298,6 +298,17 @@ class Lattice:
             getattr(self, n).copy_(ck[n])
         self.iteration = ck["iteration"]
 
+    def check_finite(self, clear: bool = True):
+        """Raise FloatingPointError if a packed fused step met a non-finite
+        density or psi since the status was last cleared, as the reference's
+        numpy step does under np.seterr(all='raise') (fingering_periodic.py:
+        496); the device status word is shared by every lattice on the device.
+        Synchronous."""
+        v = C.c_uint(0)
+        L.call("fd_device_status", C.byref(v), int(bool(clear)))
+        if v.value & L.FD_STATUS_NONFINITE:
+            raise FloatingPointError("a fused step met a non-finite density or psi")
+
     def step_seed(self) -> int:
         """Stochastic-rounding seed of the next fused launch."""
         return (self.seed + self.iteration) & 0xFFFFFFFF

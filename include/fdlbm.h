@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define FDLBM_ABI_VERSION 4
+#define FDLBM_ABI_VERSION 5
 
 enum fd_status {
   FD_OK = 0,
@@ -39,8 +39,15 @@ enum fd_status {
   FD_ERR_SHAPE = -2,    /* lattice shape not supported by this entry point */
   FD_ERR_CUDA = -3,     /* CUDA launch or runtime error */
   FD_ERR_DTYPE = -4,    /* dtype not supported by this entry point */
-  FD_ERR_SCRATCH = -5   /* request larger than a fixed scratch area */
+  FD_ERR_SCRATCH = -5,  /* request larger than a fixed scratch area */
+  FD_ERR_NONFINITE = -6 /* a step met a non-finite density or psi (the reference raises
+                           FloatingPointError there, np.seterr(all='raise'), fingering_periodic.py:496) */
 };
+
+/* Bits of the device status word (fd_device_status). */
+#define FD_STATUS_WAIT_TIMEOUT 1u /* a bounded wait on an asynchronous copy gave up */
+#define FD_STATUS_NONFINITE 2u    /* a packed fused step (fd_fused_step_packed, _host, _noalloc) met a
+                                     fluid cell whose density or psi is not finite */
 
 enum fd_dtype { FD_F64 = 0, FD_F32 = 1, FD_F16 = 2, FD_BF16 = 3 };
 
@@ -331,6 +338,16 @@ int fd_batch_step(fd_batch* b, int nsteps, int use_graph, void* stream);
 /* 0 if the members' states are in pop_a / side_a, 1 if in pop_b / side_b. */
 int fd_batch_parity(const fd_batch* b);
 
+/* Quarantine of diverging members.  Every launch checks each fluid cell's
+ * density and psi; a member with a non-finite one is flagged (out[i] != 0) and
+ * its tiles are skipped by every later launch (its state stays as it was
+ * then), while the other members keep stepping.  The reference aborts the whole
+ * run instead (np.seterr(all='raise'), fingering_periodic.py:496).  Copies the
+ * n member flags to the HOST array `out` after waiting for the device; clear
+ * != 0 then releases every member (after the caller has restored its state).
+ * Returns FD_ERR_NONFINITE if any member is flagged, FD_OK otherwise. */
+int fd_batch_member_status(fd_batch* b, uint32_t* out, int clear);
+
 /* Number of tiles per iteration. */
 int fd_batch_tiles(const fd_batch* b);
 
@@ -377,8 +394,9 @@ int fd_diagnostics(const fd_params* prm, int dtype, const fd_storage* st, const 
  * No counterpart in the reference. */
 int fd_selftest_wait_timeout(unsigned polls, int unit, void* stream);
 
-/* Device-side status word of the library's kernels (bit 0: a bounded wait on
- * an asynchronous copy gave up), the OR over the library's code units.  Copies
+/* Device-side status word of the library's kernels (FD_STATUS_* bits: a
+ * bounded wait on an asynchronous copy gave up; a packed fused step met a
+ * non-finite density or psi), the OR over the library's code units.  Copies
  * it to *out and, if clear != 0, resets it.  Synchronous.  No counterpart in the reference (numpy raises
  * instead, fingering_periodic.py:497). */
 int fd_device_status(unsigned* out, int clear);

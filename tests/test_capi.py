@@ -46,7 +46,7 @@ def test_binding_table_matches_headers():
 
 def test_abi_version_and_error_path(lib):
     from fingering_dynamics_gb300 import _lib as L
-    assert L.lib().fd_abi_version() == 4
+    assert L.lib().fd_abi_version() == 5
     # host-side argument checks run without a GPU and report through fd_last_error
     with pytest.raises(L.FDError) as e:
         L.call("fd_fused_step", None, 1, None, None, None, None, None, None, 1, 0, None)
@@ -95,6 +95,9 @@ def test_new_entry_points_check_their_arguments_on_the_host(lib):
         L.call("fd_fused_step_packed_host", ctypes.byref(prm), ctypes.byref(st), dummy, dummy, dummy, dummy,
                ctypes.c_void_p(512), ctypes.c_void_p(768), ctypes.c_void_p(1024), ctypes.c_void_p(1280), 1, 0, None)
     assert L.lib().fd_batch_grid(None) == -1 and L.lib().fd_batch_tiles(None) == -1
+    with pytest.raises(L.FDError) as e:  # no batch
+        L.call("fd_batch_member_status", None, (ctypes.c_uint32 * 1)(), 0)
+    assert e.value.code == -1
     for polls, unit in ((0, 0), (1 << 21, 0), (100, 2)):
         with pytest.raises(L.FDError) as e:
             L.call("fd_selftest_wait_timeout", polls, unit, None)
