@@ -301,31 +301,39 @@ def measure_single(prm, g, dtype, steps, warmup, rows=0, rounding="stochastic"):
             "gpu_launches_per_repetition": steps, "clocks": clk.summary()}
 
 
-def measure_ensemble(steps, warmup, members=96, dtype="f32", family="stable", seed=2024):
+ENSEMBLE_SETTLE_STEPS = 200  # before timing, so that members that diverge at once are quarantined
+
+
+def measure_ensemble(steps, warmup, members=96, dtype="f32", family="config", seed=2024):
     """The batched ensemble (seeded lattices of uneven size, geometry and
     parameters; one persistent launch per iteration replayed from a CUDA graph;
     tile shape autotuned on the ensemble): aggregate MLUPS, median over
-    repetitions of the K-step timed region."""
+    repetitions of the K-step timed region.  Members that meet a non-finite
+    cell are quarantined by the batch (skipped from then on); the value counts
+    only the cells of members still stepping at the end of the timed region."""
     import torch
     from fingering_dynamics_gb300.ensemble import Ensemble, ensemble_specs
     specs = ensemble_specs(members, seed=seed, family=family)
     ens = Ensemble([s.build() for s in specs], dtype=dtype)
+    ens.step(ENSEMBLE_SETTLE_STEPS)
+    settled = ens.member_status()
     tuned = ens.autotune(steps=10)
     ens.step(warmup)
     with ClockSampler(torch.cuda.current_device()) as clk:
         reps = timed_repetitions(lambda: ens.step(steps, use_graph=True), ens.stream)
     ms_step = statistics.median(reps) / steps
-    finite = []
-    for lat in ens.lattices:
-        d = lat.diagnostics()
-        finite.append(bool(np.isfinite(d["mass_r"]) and np.isfinite(d["mass_b"])))
+    quarantined = ens.member_status()
+    active_cells = sum(lat.H * lat.W for lat, q in zip(ens.lattices, quarantined) if not q)
     out = {"dtype": dtype, "members": members, "family": family, "cells": ens.cells,
-           "value": round(ens.cells / (ms_step / 1e3) / 1e6, 1), "unit": "MLUPS", "ms_per_step": round(ms_step, 4),
+           "active_cells": active_cells, "members_quarantined_before_timing": int(sum(settled)),
+           "members_quarantined": int(sum(quarantined)), "members_finite": members - int(sum(quarantined)),
+           "settle_steps": ENSEMBLE_SETTLE_STEPS,
+           "value": round(active_cells / (ms_step / 1e3) / 1e6, 1), "unit": "MLUPS", "ms_per_step": round(ms_step, 4),
            "timed_repetitions": len(reps), "steps_per_repetition": steps,
-           "roofline": roofline(dtype, ens.cells, ms_step),
-           "tile_shape": {"band_width": ens.config[0], "rows_per_strip": ens.config[1]},
+           "roofline": roofline(dtype, active_cells, ms_step),
+           "tile_shape": {"band_width": ens.config[0], "rows_per_strip": ens.config[1], "cells_per_thread": 1},
            "autotune_mlups": {f"{b}x{r}": round(v, 1) for (b, r), v in tuned.items()},
-           "members_finite": int(sum(finite)), "graph": True, "gpu_launches_per_repetition": steps,
+           "graph": True, "gpu_launches_per_repetition": steps,
            "clocks": clk.summary()}
     ens.close()
     del ens
@@ -460,46 +468,22 @@ def run_ours(args):
 
 
 def run_ensemble(args):
-    """The batched ensemble: 96 seeded independent lattices of uneven size,
-    geometry and parameters advanced by one persistent batched launch per
-    iteration (CUDA-graph replay), tile shape chosen by the autotuner;
-    aggregate MLUPS over all members."""
-    import torch
+    """The batched ensemble: --members seeded independent lattices of uneven
+    size, geometry and parameters (--family), advanced by one persistent
+    batched launch per iteration (CUDA-graph replay), tile shape chosen by the
+    autotuner, diverging members quarantined; aggregate MLUPS over the members
+    still stepping."""
     from fingering_dynamics_gb300 import build
-    from fingering_dynamics_gb300.ensemble import Ensemble, ensemble_specs
     build.build()
-    specs = ensemble_specs(args.members, seed=2024, family=args.family)
-    ens = Ensemble([s.build() for s in specs], dtype=args.dtype, rounding=args.rounding)
-    tuned = ens.autotune(steps=10)
-    for _ in range(args.warmup):
-        ens.step(1)
-    with ClockSampler(0) as clk:
-        secs = ens.time_steps(args.steps, use_graph=True)
-    clocks = clk.summary()
-    finite = []
-    for lat in ens.lattices:
-        d = lat.diagnostics()
-        finite.append(bool(np.isfinite(d["mass_r"]) and np.isfinite(d["mass_b"])))
-    mlups = ens.cells * args.steps / secs / 1e6
-    alg = BYTES_PER_LU[args.dtype] * ens.cells
-    peak, peak_kind = measured_peak()
-    ach = alg / (secs / args.steps) / 1e9
-    line = {"metric": "MLUPS", "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
-            "config": {"workload": f"ensemble_{args.members}_members", "members": args.members, "cells": ens.cells,
-                       "family": args.family,
-                       "rounding": args.rounding if args.dtype in ("f16", "bf16") else None,
-                       "tile_shape": {"band_width": ens.config[0], "rows_per_strip": ens.config[1]},
-                       "autotune_mlups": {f"{b}x{r}": round(v, 1) for (b, r), v in tuned.items()},
-                       "tiles_per_iteration": ens.tiles, "members_finite_after_timing": int(sum(finite)),
-                       "graph": True},
-            "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(ach / peak, 4), "peak_kind": peak_kind, "traffic": None,
-                         "algorithmic_bytes_per_launch": alg},
-            "gpu_launches": args.steps, "clocks": clocks}
+    sub = measure_ensemble(args.steps, args.warmup, members=args.members, dtype=args.dtype, family=args.family)
+    line = {"metric": "MLUPS", "value": sub["value"], "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sub["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+            "config": {"workload": f"ensemble_{args.members}_members", **{k: v for k, v in sub.items() if k not in (
+                "value", "unit", "ms_per_step", "roofline", "clocks")},
+                       "rounding": args.rounding if args.dtype in ("f16", "bf16") else None},
+            "roofline": sub["roofline"], "gpu_launches": args.steps, "clocks": sub["clocks"]}
     print(json.dumps(line), flush=True)
-    ens.close()
     return 0
 
 
@@ -729,7 +713,7 @@ def main():
     ap.add_argument("--save-net", default=None, help="surrogate: write the trained network's weights (.npz) here")
     ap.add_argument("--load-net", default=None,
                     help="accelerated: the trained network's weights (.npz, as written by --save-net)")
-    ap.add_argument("--family", default="stable", choices=["stable", "spec"],
+    ap.add_argument("--family", default="config", choices=["config", "stable", "spec"],
                     help="ensemble parameter family (spec: the configuration's literal ranges)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -91,10 +91,11 @@ def contact_angle(psi: np.ndarray, ys: float, x_center: float, min_height: float
     return math.degrees(math.acos(c))
 
 
-def calibrate(psi_walls=(-0.7, -0.5, -0.3, 0.0, 0.3, 0.5, 0.7), steps: int = 8000, dtype: str = "f32") -> dict:
+def calibrate(psi_walls=(-0.7, -0.5, -0.3, 0.0, 0.3, 0.5, 0.7), steps: int = 8000, dtype: str = "f32",
+              H: int = 128, W: int = 256, radius: int = 24, substrate: int = 24) -> dict:
     """Run one droplet per psi_wall (one batched ensemble) and measure angles."""
     from .ensemble import Ensemble
-    cases = [droplet_case(pw) for pw in psi_walls]
+    cases = [droplet_case(pw, H=H, W=W, radius=radius, substrate=substrate) for pw in psi_walls]
     ens = Ensemble([(p, g, psi0) for p, g, psi0, _ in cases], dtype=dtype)
     ens.step(steps)
     angles = []
@@ -103,7 +104,8 @@ def calibrate(psi_walls=(-0.7, -0.5, -0.3, 0.0, 0.3, 0.5, 0.7), steps: int = 800
         angles.append(contact_angle(psi, ys, prm.W / 2))
     ens.close()
     return {"psi_wall": [float(p) for p in psi_walls], "theta_deg": angles, "steps": steps,
-            "setup": "128x256 periodic variant, reference constants, M = 1, no inflow, droplet R = 24 on a block"}
+            "setup": f"{H}x{W} periodic variant, reference constants, M = 1, no inflow, droplet R = {radius} on a "
+                     f"block up to row {substrate}"}
 
 
 def psi_wall_for_angle(theta_deg: float, table: dict | None = None) -> float:

@@ -28,9 +28,11 @@ DEFAULT_CANDIDATES = ((128, 16), (128, 32), (128, 64), (64, 32), (64, 64), (256,
 class MemberSpec:
     """One seeded ensemble member.
 
-    family "spec": lattice parameters from relaxation times (tau_def = 1.0,
-    tau_inv from the viscosity ratio), interfacial tension ``sigma``, psi_wall =
-    cos(contact angle) and the reference's mobility rule.  family "stable": the
+    family "spec" (and "config", the same parameterisation over narrower
+    porosity and inlet ranges): lattice parameters from relaxation times
+    (tau_def = 1.0, tau_inv from the viscosity ratio), interfacial tension
+    ``sigma``, psi_wall from the contact angle through the droplet calibration
+    table and the reference's mobility rule.  family "stable": the
     constants of fingering.py:16-50 with the viscosity ratio, psi_wall and inlet
     speed of this member.  The reference model diverges within tens of steps
     for much of the "spec" ranges on dense random obstacles (tau_inv -> 0.525,
@@ -73,14 +75,21 @@ def ensemble_specs(n: int, seed: int, sizes_w=(256, 512, 1024, 2048), sizes_h=(1
 
     Family "spec" defaults to the ranges of the benchmark configuration
     (viscosity ratio 2..20, porosity 0.6..0.85, inlet 0.005..0.02).  Family
+    "config" keeps that configuration's viscosity-ratio, contact-angle and
+    interfacial-tension ranges and narrows only porosity (0.70..0.85) and
+    inlet speed (0.003..0.010), the two ranges whose upper / lower ends the
+    Darcy argument below rules out; members that still diverge are
+    quarantined by the batch (Ensemble.member_status).  Family
     "stable" defaults to viscosity ratio 2..5, porosity 0.70..0.85 and inlet
     0.003..0.010: the medium must carry the imposed flux with density
     differences of order 3 u nu L / k (Darcy), and denser or faster members
     diverge within a few thousand steps (with either outlet rule); on the
     96-member draw of seed 2024 none of these diverges within 6000 steps,
     against 35 of 96 with the configuration's porosity and inlet ranges."""
+    if family not in ("spec", "config", "stable"):
+        raise ValueError(f"unknown ensemble family {family!r}")
     if ratio is None:
-        ratio = (2.0, 20.0) if family == "spec" else (2.0, 5.0)
+        ratio = (2.0, 20.0) if family in ("spec", "config") else (2.0, 5.0)
     if porosity is None:
         porosity = (0.6, 0.85) if family == "spec" else (0.70, 0.85)
     if u_in is None:

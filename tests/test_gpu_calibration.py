@@ -28,3 +28,22 @@ def test_droplet_angles_monotone_and_table_consistent():
             assert abs(t - ref) < 6.0, (pw, t, ref)
     # the inverse map reproduces the table
     assert abs(psi_wall_for_angle(table["theta_deg"][3], table) - table["psi_wall"][3]) < 1e-6
+
+
+def test_gpu_droplet_angles_match_the_oracle():
+    """The calibration experiment on the GPU (batched FP32 kernels) against the
+    same experiment in the FP64 CPU oracle (tests/golden/droplet_angles_64x128.json,
+    made by tests/golden/make_droplet_angles.py): 64 x 128, droplet R = 12,
+    2000 iterations, psi_wall in {-0.5, 0, 0.5}; angles within 1.5 degrees."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fingering_dynamics_gb300 import build
+    build.build()
+    from fingering_dynamics_gb300.calibration import calibrate
+    from golden.make_droplet_angles import OUT
+    with open(OUT) as fh:
+        gold = json.load(fh)
+    res = calibrate(psi_walls=tuple(gold["psi_wall"]), steps=gold["steps"], H=gold["H"], W=gold["W"],
+                    radius=gold["radius"], substrate=gold["substrate"])
+    for pw, t, ref in zip(gold["psi_wall"], res["theta_deg"], gold["theta_deg"]):
+        assert abs(t - ref) < 1.5, (pw, t, ref)
