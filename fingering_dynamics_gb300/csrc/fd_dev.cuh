@@ -104,6 +104,33 @@ __device__ __forceinline__ uint32_t sr_next(uint32_t s) { return s * 1664525u + 
 // the FP32 pattern, then truncate.  (Below the FP16 normal range, 6.1e-5, more
 // bits are discarded than dithered: there the rounding leans towards zero by
 // at most one FP16 subnormal step, 6e-8.)
+// Two values to the storage type in one conversion: the 32-bit word holds lo in
+// its low half and hi in its high half (cvt.rn / cvt.rs .f16x2 / .bf16x2; the
+// stochastic form rounds each value up with probability equal to its discarded
+// fraction, from the 32 random bits r, different bits for the two values).
+template <typename S> __device__ __forceinline__ uint32_t pair_from_f(float lo, float hi);
+template <> __device__ __forceinline__ uint32_t pair_from_f<__half>(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+template <> __device__ __forceinline__ uint32_t pair_from_f<__nv_bfloat16>(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+template <typename S> __device__ __forceinline__ uint32_t pair_from_f_sr(float lo, float hi, uint32_t r);
+template <> __device__ __forceinline__ uint32_t pair_from_f_sr<__half>(float lo, float hi, uint32_t r) {
+  uint32_t d;
+  asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(r));
+  return d;
+}
+template <> __device__ __forceinline__ uint32_t pair_from_f_sr<__nv_bfloat16>(float lo, float hi, uint32_t r) {
+  uint32_t d;
+  asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(r));
+  return d;
+}
+
 template <typename S> __device__ __forceinline__ S from_f_sr(float v, uint32_t r);
 template <> __device__ __forceinline__ float from_f_sr<float>(float v, uint32_t) { return v; }
 template <> __device__ __forceinline__ __half from_f_sr<__half>(float v, uint32_t r) {
@@ -176,6 +203,20 @@ __device__ __forceinline__ float dev_mu(const DevCoef& c, const DevStencil& s) {
   return c.a * s.psi * s.omp - c.kappa * s.lap;
 }
 
+// 1 / x rounded to nearest, or (FAST) the hardware approximation (at most
+// 1 ulp from it), used where the populations are stored in FP16/BF16
+template <bool FAST>
+__device__ __forceinline__ float dev_rcp(float x) {
+  if constexpr (FAST) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  } else {
+    return __frcp_rn(x);
+  }
+}
+
+template <bool FAST_RCP = false>
 __device__ __forceinline__ DevMacro dev_macros(const DevCoef& c, const float (&d)[9], const DevStencil& st) {
   DevMacro m;
   m.drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
@@ -187,11 +228,11 @@ __device__ __forceinline__ DevMacro dev_macros(const DevCoef& c, const float (&d
   m.gx = gx;
   m.gy = gy;
   m.mu = dev_mu(c, st);  // getMu (fingering_periodic.py:141-144)
-  const float inv_rho = __frcp_rn(m.rho);
+  const float inv_rho = dev_rcp<FAST_RCP>(m.rho);
   m.ux = fmaf(0.5f * m.mu, gx, jx) * inv_rho;             // getUx (fingering_periodic.py:126-132)
   m.uy = fmaf(0.5f * m.mu, gy, jy) * inv_rho;
   const float rD = m.rho * fmaf(c.eta_diff, psi, c.eta_sum);
-  m.inv_tau = rD * __frcp_rn(fmaf(0.5f, rD, c.six_eta_prod));  // 1 / getMix_tau
+  m.inv_tau = rD * dev_rcp<FAST_RCP>(fmaf(0.5f, rD, c.six_eta_prod));  // 1 / getMix_tau
   m.pref = m.mu * fmaf(-0.5f, m.inv_tau, 1.0f);              // mu (1 - 1/(2 tau))
   return m;
 }

@@ -317,6 +317,50 @@ __device__ __forceinline__ unsigned mask_at(const char* sm, int mrow, int lx) {
 // psi of cell x (band index lx) of row y from its pulled g after Zou-He
 // (fingering_periodic.py:210-212, 278-302); the pulled g is returned in g.
 // `mrow` is the byte offset of row y's mask row.
+
+// Stores of one cell's new populations into the packed layout (q = y W + x).
+// FP16/BF16: the 17 values in the storage type (f_0..f_8 then g_1..g_8) are
+// converted two at a time with one instruction (pair_from_f, pair_from_f_sr:
+// one 32-bit random word per pair) and written as 16-bit stores; g_0 stays FP32.
+template <typename SF, bool SCALED, bool STOCH>
+__device__ __forceinline__ void store_cell(const DevArgs<SF>& a, size_t q, const float (&f)[9], const float (&g)[9]) {
+  if constexpr (std::is_same_v<SF, float>) {
+    float* pf = a.dst_f + q;
+#pragma unroll
+    for (int i = 0; i < 9; ++i, pf += a.pstride_f) *pf = f[i];
+    a.dst_g0[q] = g[0];
+    float* pg = a.dst_gi + q;
+#pragma unroll
+    for (int i = 1; i < 9; ++i, pg += a.pstride_f) *pg = g[i];
+  } else {
+    float v[18];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) v[i] = SCALED ? f[i] * a.c.sf : f[i];
+#pragma unroll
+    for (int i = 1; i < 9; ++i) v[8 + i] = SCALED ? g[i] * a.c.sg : g[i];
+    v[17] = 0.0f;
+    uint32_t rs = 0;
+    if constexpr (STOCH) rs = sr_hash((uint32_t)q ^ a.seed);
+    auto plane = [&](int k) -> uint16_t* {
+      SF* p = k < 9 ? a.dst_f + (size_t)k * a.pstride_f + q : a.dst_gi + (size_t)(k - 9) * a.pstride_f + q;
+      return reinterpret_cast<uint16_t*>(p);
+    };
+#pragma unroll
+    for (int k = 0; k < 17; k += 2) {
+      uint32_t w;
+      if constexpr (STOCH) {
+        rs = sr_next(rs);
+        w = pair_from_f_sr<SF>(v[k], v[k + 1], rs);
+      } else {
+        w = pair_from_f<SF>(v[k], v[k + 1]);
+      }
+      *plane(k) = (uint16_t)w;
+      if (k + 1 < 17) *plane(k + 1) = (uint16_t)(w >> 16);
+    }
+    a.dst_g0[q] = g[0];
+  }
+}
+
 // With paired psi (psi_paired) the result is the pair (hi, lo), else (psi, 0).
 template <typename SF, int NT, bool SCALED>
 __device__ __forceinline__ float2 psi_cell(const char* sm, const DevArgs<SF>& a, const int (&rows)[3], int mrow, int x,
@@ -489,33 +533,11 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
         a.side_out[(o + 2) * a.H + y] = dev_mu(a.c, st);
       }
       if (!(m & SOLID)) {
-        const DevMacro mc = dev_macros(a.c, f, st);
+        const DevMacro mc = dev_macros<!std::is_same_v<SF, float>>(a.c, f, st);
         bad |= nonfinite_cell(mc.rho, mc.psi);
         dev_collide(a.c, mc, f, gC);
       }
-      const size_t q = (size_t)y * a.W + x;
-      uint32_t rs = 0;  // stochastic rounding state of this cell (fd_dev.cuh)
-      if constexpr (STOCH) rs = sr_hash((uint32_t)q ^ a.seed);
-      auto put = [&](SF* p, float v, float scale) {
-        if constexpr (std::is_same_v<SF, float>) {
-          *p = v;
-        } else {
-          if constexpr (SCALED) v *= scale;
-          if constexpr (STOCH) {
-            rs = sr_next(rs);
-            *p = from_f_sr<SF>(v, rs);
-          } else {
-            *p = from_f<SF>(v);
-          }
-        }
-      };
-      SF* pf = a.dst_f + q;
-#pragma unroll
-      for (int i = 0; i < 9; ++i, pf += a.pstride_f) put(pf, f[i], a.c.sf);
-      a.dst_g0[q] = gC[0];
-      SF* pg = a.dst_gi + q;
-#pragma unroll
-      for (int i = 1; i < 9; ++i, pg += a.pstride_f) put(pg, gC[i], a.c.sg);
+      store_cell<SF, SCALED, STOCH>(a, (size_t)y * a.W + x, f, gC);
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) gC[i] = gN[i];
@@ -691,33 +713,11 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
         a.side_out[(o + 2) * a.H + y] = dev_mu(a.c, st);
       }
       if (!(m & SOLID)) {
-        const DevMacro mc = dev_macros(a.c, f, st);
+        const DevMacro mc = dev_macros<!std::is_same_v<SF, float>>(a.c, f, st);
         bad |= nonfinite_cell(mc.rho, mc.psi);
         dev_collide(a.c, mc, f, gC);
       }
-      const size_t q = (size_t)y * a.W + x;
-      uint32_t rs = 0;  // stochastic rounding state of this cell (fd_dev.cuh)
-      if constexpr (STOCH) rs = sr_hash((uint32_t)q ^ a.seed);
-      auto put = [&](SF* p, float v, float scale) {
-        if constexpr (std::is_same_v<SF, float>) {
-          *p = v;
-        } else {
-          if constexpr (SCALED) v *= scale;
-          if constexpr (STOCH) {
-            rs = sr_next(rs);
-            *p = from_f_sr<SF>(v, rs);
-          } else {
-            *p = from_f<SF>(v);
-          }
-        }
-      };
-      SF* pf = a.dst_f + q;
-#pragma unroll
-      for (int i = 0; i < 9; ++i, pf += a.pstride_f) put(pf, f[i], a.c.sf);
-      a.dst_g0[q] = gC[0];
-      SF* pg = a.dst_gi + q;
-#pragma unroll
-      for (int i = 1; i < 9; ++i, pg += a.pstride_f) put(pg, gC[i], a.c.sg);
+      store_cell<SF, SCALED, STOCH>(a, (size_t)y * a.W + x, f, gC);
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) gC[i] = gN[i];
