@@ -21,9 +21,6 @@ from .geometry import build_geometry, random_blocks
 from .lattice import Lattice
 from .params import LBMParams, from_relaxation_times, walls_reference_params
 
-# f relaxation time of the invading fluid in the "config" family (the defending
-# fluid's follows from the viscosity ratio); the single-lattice workload uses it too
-CONFIG_TAU_INV = 0.6
 DEFAULT_CANDIDATES = ((128, 16), (128, 32), (128, 64), (64, 32), (64, 64), (256, 16), (256, 32))
 
 
@@ -31,13 +28,11 @@ DEFAULT_CANDIDATES = ((128, 16), (128, 32), (128, 64), (64, 32), (64, 64), (256,
 class MemberSpec:
     """One seeded ensemble member.
 
-    family "spec": lattice parameters from relaxation times (tau_def = 1.0,
-    tau_inv from the viscosity ratio), interfacial tension ``sigma``, psi_wall
-    from the contact angle through the droplet calibration table and the
-    reference's mobility rule.  Family "config": the same with tau_inv = 0.6
-    and tau_def = 0.5 + 0.1 M, so the viscosity ratio M keeps its range while
-    tau_inv stays where the model runs (with tau_def = 1.0, every member whose
-    tau_inv fell below 0.575, i.e. M > 6.6, diverged within 50 iterations).  family "stable": the
+    family "spec" (and "config", the same parameterisation over narrower
+    porosity and inlet ranges): lattice parameters from relaxation times
+    (tau_def = 1.0, tau_inv from the viscosity ratio), interfacial tension
+    ``sigma``, psi_wall from the contact angle through the droplet calibration
+    table and the reference's mobility rule.  family "stable": the
     constants of fingering.py:16-50 with the viscosity ratio, psi_wall and inlet
     speed of this member.  The reference model diverges within tens of steps
     for much of the "spec" ranges on dense random obstacles (tau_inv -> 0.525,
@@ -59,10 +54,6 @@ class MemberSpec:
             prm = walls_reference_params().with_size(self.H, self.W)
             return replace(prm, M=self.viscosity_ratio, psi_wall=self.psi_wall, u0=self.u_in,
                            inlet_ux=np.full(self.H, self.u_in))
-        if self.family == "config":
-            tau_inv = CONFIG_TAU_INV
-            return from_relaxation_times(self.H, self.W, tau_inv, 0.5 + self.viscosity_ratio * (tau_inv - 0.5),
-                                         self.sigma, self.contact_angle_deg, self.u_in, variant=variant)
         tau_inv = 0.5 + (tau_def - 0.5) / self.viscosity_ratio
         return from_relaxation_times(self.H, self.W, tau_inv, tau_def, self.sigma, self.contact_angle_deg,
                                      self.u_in, variant=variant)
@@ -85,8 +76,7 @@ def ensemble_specs(n: int, seed: int, sizes_w=(256, 512, 1024, 2048), sizes_h=(1
     Family "spec" defaults to the ranges of the benchmark configuration
     (viscosity ratio 2..20, porosity 0.6..0.85, inlet 0.005..0.02).  Family
     "config" keeps that configuration's viscosity-ratio, contact-angle and
-    interfacial-tension ranges (viscosity ratio through tau_def, MemberSpec)
-    and narrows porosity (0.70..0.85) and inlet speed (0.003..0.010), the two
+    interfacial-tension ranges and narrows porosity (0.70..0.85) and inlet speed (0.003..0.010), the two
     ranges whose upper / lower ends the Darcy argument below rules out;
     members that still diverge are quarantined by the batch
     (Ensemble.member_status).  Family
