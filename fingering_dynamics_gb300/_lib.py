@@ -77,6 +77,7 @@ SIGNATURES = {
     "fd_last_error": [],
     "fd_compute_init": [_P, _I, _VP, _VP, _VP, _F, _VP],
     "fd_collide": [_P, _I, _VP, _F, _VP],
+    "fd_add_nonequilibrium": [_P, _I, _VP, _F, _VP],
     "fd_collision_term": [_P, _I, _I, _I, _VP, _F, _VP, _VP],
     "fd_stream": [_P, _I, _VP, _VP, _VP, _VP, _VP],
     "fd_bounce_back": [_P, _I, _VP, _VP, _VP, _VP, _VP, _VP],

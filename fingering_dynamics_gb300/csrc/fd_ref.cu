@@ -128,6 +128,64 @@ __global__ void k_init_rest(Shape s, Coef<T> c, unsigned flags, const uint16_t* 
   for (int i = 0; i < 9; ++i) { F.f[i * s.P + q] = feq[i]; F.g[i * s.P + q] = geq[i]; }
 }
 
+// --- first-order non-equilibrium part of a restart (no reference counterpart) ---
+// A state rebuilt from fields (fd_compute_init with FD_INIT_VELOCITY) is the
+// equilibrium of those fields; a flow with velocity gradients also carries the
+// first-order Chapman-Enskog part of its populations.  This kernel adds it:
+//   f_i += -3 w_i tau_mix Q_i : S(rho u),   g_i += -3 w_i tau Q_i : S(psi u)
+// with Q_i = e_i e_i - I/3 and S(v) the symmetric part of grad v from central
+// differences over fluid neighbours (one-sided next to solid cells or the x
+// edges, zero where neither neighbour is fluid).  sum_i w_i Q_i = 0 and
+// sum_i w_i Q_i e_i = 0, so density, psi and momentum are unchanged.  Fluid
+// cells only; fields must hold rho, psi, ux, uy, mix_tau of the state.
+template <typename T>
+__global__ void k_nonequilibrium(Shape s, Coef<T> c, const uint16_t* __restrict__ mask, Fields<T> F) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= s.P || (mask[q] & SOLID)) return;
+  const int x = (int)(q % s.W), y = (int)(q / s.W);
+  // (rho u, psi u) at a neighbour, false if it is solid or outside the lattice
+  auto flux = [&](int xx, int yy, T (&v)[4]) -> bool {
+    if (yy < 0 || yy >= s.H) {
+      if (s.variant == FD_VARIANT_WALLS) return false;
+      yy = wrap(yy, s.H);
+    }
+    if (xx < 0 || xx >= s.W) {
+      if (s.variant != FD_VARIANT_PERIODIC_XY) return false;
+      xx = wrap(xx, s.W);
+    }
+    const size_t k = (size_t)yy * s.W + xx;
+    if (mask[k] & SOLID) return false;
+    v[0] = F.rho[k] * F.ux[k];
+    v[1] = F.rho[k] * F.uy[k];
+    v[2] = F.psi[k] * F.ux[k];
+    v[3] = F.psi[k] * F.uy[k];
+    return true;
+  };
+  T vc[4], vp[4], vm[4], dx[4], dy[4];
+  flux(x, y, vc);
+  const bool xp = flux(x + 1, y, vp), xm = flux(x - 1, y, vm);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    dx[k] = (xp && xm) ? T(0.5) * (vp[k] - vm[k]) : xp ? vp[k] - vc[k] : xm ? vc[k] - vm[k] : T(0);
+  const bool yp = flux(x, y + 1, vp), ym = flux(x, y - 1, vm);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    dy[k] = (yp && ym) ? T(0.5) * (vp[k] - vm[k]) : yp ? vp[k] - vc[k] : ym ? vc[k] - vm[k] : T(0);
+  // S of rho u (index 0/1) and of psi u (2/3)
+  const T fxx = dx[0], fyy = dy[1], fxy = T(0.5) * (dy[0] + dx[1]);
+  const T gxx = dx[2], gyy = dy[3], gxy = T(0.5) * (dy[2] + dx[3]);
+  const T tf = F.mix_tau[q], tg = T(1) / c.tau_inv;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const T ex = (T)ex_of(i), ey = (T)ey_of(i);
+    const T qxx = ex * ex - T(1) / T(3), qyy = ey * ey - T(1) / T(3), qxy = ex * ey;
+    const T qsf = qxx * fxx + qyy * fyy + T(2) * qxy * fxy;
+    const T qsg = qxx * gxx + qyy * gyy + T(2) * qxy * gxy;
+    F.f[i * s.P + q] += T(-3) * c.w[i] * tf * qsf;
+    F.g[i * s.P + q] += T(-3) * c.w[i] * tg * qsg;
+  }
+}
+
 // --- collision (fingering_periodic.py:455-460) -----------------------------
 template <typename T>
 __global__ void k_collide(Shape s, Coef<T> c, const uint16_t* __restrict__ mask, Fields<T> F) {
@@ -370,6 +428,13 @@ int launch_init(const fd_params& p, const uint16_t* mask, const double* psi0, co
 }
 
 template <typename T>
+int launch_nonequilibrium(const fd_params& p, const uint16_t* mask, const fd_fields& fl, cudaStream_t st) {
+  const Shape s = shape_of(p);
+  k_nonequilibrium<T><<<grid_cells(s), kBlock, 0, st>>>(s, make_coef<T>(p), mask, typed<T>(fl));
+  return check_launch("fd_add_nonequilibrium");
+}
+
+template <typename T>
 int launch_collide(const fd_params& p, const uint16_t* mask, const fd_fields& fl, cudaStream_t st) {
   const Shape s = shape_of(p);
   k_collide<T><<<grid_cells(s), kBlock, 0, st>>>(s, make_coef<T>(p), mask, typed<T>(fl));
@@ -473,6 +538,15 @@ int fd_compute_init(const fd_params* prm, int dtype, const uint16_t* mask, const
   FD_REQUIRE(mask && psi0 && fields_ok(out), FD_ERR_ARG, "fd_compute_init: NULL pointer");
   return dtype == FD_F64 ? launch_init<double>(*prm, mask, psi0, rho0, *out, as_stream(stream))
                          : launch_init<float>(*prm, mask, psi0, rho0, *out, as_stream(stream));
+}
+
+int fd_add_nonequilibrium(const fd_params* prm, int dtype, const uint16_t* mask, const fd_fields* fields,
+                          void* stream) {
+  if (int r = check_params(prm)) return r;
+  if (int r = check_dtype(dtype)) return r;
+  FD_REQUIRE(mask && fields_ok(fields), FD_ERR_ARG, "fd_add_nonequilibrium: NULL pointer");
+  return dtype == FD_F64 ? launch_nonequilibrium<double>(*prm, mask, *fields, as_stream(stream))
+                         : launch_nonequilibrium<float>(*prm, mask, *fields, as_stream(stream));
 }
 
 int fd_collide(const fd_params* prm, int dtype, const uint16_t* mask, const fd_fields* fields, void* stream) {

@@ -259,11 +259,14 @@ class Lattice:
                _ptr(self.pop[self.cur]), self._stream())
         self._finish_from(self.pop[self.cur], self.side[self.scur], self.pop[1 - self.cur])
 
-    def restart_from_fields(self, psi, ux, uy, rho=None, iteration: int | None = None):
+    def restart_from_fields(self, psi, ux, uy, rho=None, iteration: int | None = None,
+                            regularised: bool = False):
         """Replace the state by the equilibrium of the given fields ((H, W)
         device tensors or arrays): populations f = feq(rho, u, psi, mu(psi)),
         g = geq, as Compute.__init__ builds them (fingering_periodic.py:
-        100-121) but with the given velocity (FD_INIT_VELOCITY).  Leaves the
+        100-121) but with the given velocity (FD_INIT_VELOCITY); with
+        ``regularised`` also the first-order non-equilibrium part of the
+        flow's velocity gradients (fd_add_nonequilibrium).  Leaves the
         lattice in reference mode at ``iteration`` (default: unchanged)."""
         dev, td = self.device, self.tdtype
         self.mode = "reference"
@@ -277,6 +280,9 @@ class Lattice:
         # reuses their memory only for work ordered after the init kernels
         L.call("fd_compute_init", C.byref(prm), self.fd_dtype, _ptr(self.mask), _ptr(psi_d), _ptr(rho_d),
                C.byref(self.fields()), self._stream())
+        if regularised:
+            L.call("fd_add_nonequilibrium", C.byref(prm), self.fd_dtype, _ptr(self.mask), C.byref(self.fields()),
+                   self._stream())
         if iteration is not None:
             self.iteration = int(iteration)
 

@@ -487,7 +487,7 @@ def rollout(net: UNet, lat, jumps_per_check: int = 5, checks: int = 4, jump: int
 
 
 def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int = 5, jump: int = 200,
-                         tol: float = 0.02, dtype: str = "f32") -> dict:
+                         tol: float = 0.02, dtype: str = "f32", restart: str = "regularised") -> dict:
     """The surrogate-accelerated ensemble against the plain batched LBM over
     the same horizon, rounds x (jumps_per_check + 1) x jump iterations.
 
@@ -499,10 +499,17 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
     own prediction for that iteration by more than `tol` (relative) is put
     back to its state at the round's start (exactly) and advanced by plain
     batched LBM instead.  Returns wall times, final saturations and
-    acceptance."""
+    acceptance.  ``restart``: "regularised" (equilibrium plus the first-order
+    non-equilibrium part of the predicted flow, fd_add_nonequilibrium) or
+    "equilibrium".  The plain run is advanced round by round, so each round's
+    plain saturations are known: the record gives, for the member-rounds the
+    judge accepted, the saturation error against the plain run at the end of
+    the round (how well the judge's self-consistency test tracks the truth)."""
     from .ensemble import Ensemble
     from .lattice import Lattice
 
+    if restart not in ("regularised", "equilibrium"):
+        raise ValueError("restart must be 'regularised' or 'equilibrium'")
     span = (jumps_per_check + 1) * jump
     horizon = rounds * span
 
@@ -535,12 +542,17 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
         return v.tolist()
 
     plain = [Lattice(p, g, dtype=dtype) for p, g in members]
+    plain_batch = batch(plain)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    advance(plain, horizon)
+    sat_plain_rounds = []
+    for _ in range(rounds):
+        advance(plain, span, plain_batch)
+        sat_plain_rounds.append(sats(plain))
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t0
-    sat_plain = sats(plain)
+    plain_batch.close()
+    sat_plain = sat_plain_rounds[-1]
     del plain
     torch.cuda.empty_cache()
 
@@ -559,7 +571,8 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
         tick = now
 
     judge = None  # the batch over all members, built at the first judge
-    for _ in range(rounds):
+    accepted_err = []  # saturation error against the plain run of accepted member-rounds, at the round's end
+    for rnd in range(rounds):
         ck = [lat.checkpoint() for lat in lats]
         lap("checkpoint")
         x = torch.stack([frame_from_fields(lat.psi, lat.ux, lat.uy, ~lat.fluid) for lat in lats]).contiguous()
@@ -572,7 +585,8 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
         for m, lat in enumerate(lats):
             psi, ux, uy = fields_from_frame(x[m])
             lat.restart_from_fields(torch.where(lat.fluid, psi, lat.params.psi_wall), ux, uy, rho=lat.rho,
-                                    iteration=lat.iteration + jumps_per_check * jump)
+                                    iteration=lat.iteration + jumps_per_check * jump,
+                                    regularised=restart == "regularised")
         lap("restart")
         if judge is None:
             judge = batch(lats)
@@ -581,6 +595,9 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
         for m, s_lbm in enumerate(sats(lats)):
             if np.isfinite(s_lbm) and abs(s_lbm - sat_sur[m]) <= tol * max(s_lbm, 1e-12):
                 accepted += 1
+                sp = sat_plain_rounds[rnd][m]
+                if np.isfinite(sp) and sp > 0:
+                    accepted_err.append(abs(s_lbm - sp) / sp)
             else:
                 rejected.append(m)
         lap("judge")
@@ -602,6 +619,108 @@ def accelerated_ensemble(net: UNet, members, rounds: int, jumps_per_check: int =
             "plain_s": t_plain, "accelerated_s": t_acc, "speedup": t_plain / t_acc,
             "accelerated_phase_s": {k: round(v, 4) for k, v in phase.items()},
             "accepted_rounds": accepted, "member_rounds": rounds * len(members),
-            "members_compared": len(ok),
+            "members_compared": len(ok), "restart": restart,
             "final_saturation_rel_error_mean": float(np.mean(rel)) if rel else None,
-            "final_saturation_rel_error_max": float(np.max(rel)) if rel else None}
+            "final_saturation_rel_error_max": float(np.max(rel)) if rel else None,
+            "accepted_vs_plain_rel_error_mean": float(np.mean(accepted_err)) if accepted_err else None,
+            "accepted_vs_plain_rel_error_max": float(np.max(accepted_err)) if accepted_err else None}
+
+
+def breakthrough_race(net: UNet, members, max_rounds: int, jumps_per_check: int = 5, jump: int = 200,
+                      tol: float = 0.02, dtype: str = "f32", restart: str = "regularised") -> dict:
+    """Plain batched LBM against the surrogate-accelerated ensemble, each run
+    until every member has broken through (invading fluid within five columns
+    of the outlet: fd_diag.breakthrough) or `max_rounds` rounds of
+    (jumps_per_check + 1) x jump iterations have passed.  Each round of the
+    accelerated run is a round of accelerated_ensemble (jumps, restart, LBM
+    judge, plain replay of rejected members).  Breakthrough is checked at the
+    end of every round in both runs.  Returns per member the iteration and the
+    wall time of breakthrough in either run, and the wall time until the last
+    member that broke through in the plain run broke through in each."""
+    from .ensemble import Ensemble
+    from .lattice import Lattice
+
+    span = (jumps_per_check + 1) * jump
+
+    def batch(lats):
+        sms = torch.cuda.get_device_properties(lats[0].device).multi_processor_count
+        band_rows = sum(-(-lat.W // 128) * lat.H for lat in lats)
+        rows = int(min(64, max(8, -(-band_rows // (5 * sms)))))
+        return Ensemble.from_lattices(lats, rows_per_strip=rows, band_width=128)
+
+    def advance(lats, n, ens):
+        for lat in lats:
+            lat.enter_fused()
+        ens.step(n - 1)
+        for lat in lats:
+            lat.exit_fused()
+
+    def through(lats):
+        return [bool(lat.diagnostics()["breakthrough"]) for lat in lats]
+
+    n = len(members)
+    res = {}
+    for mode in ("plain", "accelerated"):
+        lats = [Lattice(p, g, dtype=dtype) for p, g in members]
+        ens = batch(lats)
+        hit_it = [None] * n
+        hit_s = [None] * n
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rounds = 0
+        for rounds in range(1, max_rounds + 1):
+            if mode == "plain":
+                advance(lats, span, ens)
+            else:
+                ck = [lat.checkpoint() for lat in lats]
+                x = torch.stack([frame_from_fields(lat.psi, lat.ux, lat.uy, ~lat.fluid) for lat in lats]).contiguous()
+                for _ in range(jumps_per_check):
+                    x = net.predict(x)
+                nxt = net.predict(x)
+                fl = nxt[..., 3] == 0
+                sat_sur = (((nxt[..., 0].float() > 0) & fl).sum(dim=(1, 2)).float()
+                           / fl.sum(dim=(1, 2)).float()).tolist()
+                for m, lat in enumerate(lats):
+                    psi, ux, uy = fields_from_frame(x[m])
+                    lat.restart_from_fields(torch.where(lat.fluid, psi, lat.params.psi_wall), ux, uy, rho=lat.rho,
+                                            iteration=lat.iteration + jumps_per_check * jump,
+                                            regularised=restart == "regularised")
+                advance(lats, jump, ens)
+                sat_lbm = [float(((lat.psi > 0) & lat.fluid).sum() / lat.fluid.sum().clamp(min=1)) for lat in lats]
+                rejected = [m for m in range(n) if not (np.isfinite(sat_lbm[m]) and abs(sat_lbm[m] - sat_sur[m])
+                                                        <= tol * max(sat_lbm[m], 1e-12))]
+                for m in rejected:
+                    lats[m].restore(ck[m])
+                if rejected:
+                    sub = [lats[m] for m in rejected]
+                    tmp = batch(sub)
+                    advance(sub, span, tmp)
+                    tmp.close()
+            flags = through(lats)
+            now = time.perf_counter() - t0
+            for m in range(n):
+                if flags[m] and hit_it[m] is None:
+                    hit_it[m], hit_s[m] = rounds * span, now
+            if all(h is not None for h in hit_it):
+                break
+        ens.close()
+        res[mode] = {"breakthrough_iteration": hit_it, "breakthrough_s": hit_s, "rounds": rounds}
+        del lats
+        torch.cuda.empty_cache()
+    both = [m for m in range(n) if res["plain"]["breakthrough_s"][m] is not None
+            and res["accelerated"]["breakthrough_s"][m] is not None]
+    out = {"members": n, "span_iterations": span, "max_rounds": max_rounds, "restart": restart,
+           "plain": res["plain"], "accelerated": res["accelerated"],
+           "members_through_plain": sum(h is not None for h in res["plain"]["breakthrough_s"]),
+           "members_through_accelerated": sum(h is not None for h in res["accelerated"]["breakthrough_s"]),
+           "members_through_both": len(both)}
+    if both:
+        tp = max(res["plain"]["breakthrough_s"][m] for m in both)
+        ta = max(res["accelerated"]["breakthrough_s"][m] for m in both)
+        out["time_to_last_breakthrough_plain_s"] = tp
+        out["time_to_last_breakthrough_accelerated_s"] = ta
+        out["breakthrough_speedup"] = tp / ta
+        it_err = [abs(res["accelerated"]["breakthrough_iteration"][m] - res["plain"]["breakthrough_iteration"][m])
+                  / res["plain"]["breakthrough_iteration"][m] for m in both]
+        out["breakthrough_iteration_rel_error_mean"] = float(np.mean(it_err))
+    return out

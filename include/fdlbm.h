@@ -132,6 +132,17 @@ const char* fd_last_error(void);
 int fd_compute_init(const fd_params* prm, int dtype, const uint16_t* mask, const double* psi0,
                     const double* rho0, const fd_fields* out, void* stream);
 
+/* Regularised restart (no counterpart in the reference, whose runs start at
+ * rest): adds to populations that hold the equilibrium of given fields (as
+ * fd_compute_init with FD_INIT_VELOCITY writes them) the first-order
+ * non-equilibrium part of that flow, f_i += -3 w_i tau_mix Q_i : S(rho u) and
+ * g_i += -3 w_i tau Q_i : S(psi u), Q_i = e_i e_i - I/3, S the symmetric
+ * velocity-flux gradient by central differences over fluid neighbours.  Density,
+ * psi and momentum are unchanged.  Fluid cells only; `fields` holds rho, psi,
+ * ux, uy and mix_tau of the state (as fd_compute_init leaves them). */
+int fd_add_nonequilibrium(const fd_params* prm, int dtype, const uint16_t* mask, const fd_fields* fields,
+                          void* stream);
+
 /* The collision loop body for all nine directions, fluid cells only:
  * f[j][mask] = getF(j), g[j][mask] = getG(j) with F, feq, geq from the stored
  * fields (fingering_periodic.py:455-460). In place on fields->f, fields->g. */

@@ -475,3 +475,49 @@ def diagnostics(st: OracleState) -> dict:
         "tip_x": int(xs[inv].max()) if inv.any() else -1,
         "breakthrough": int(bool(inv[xs >= st.prm.W - 5].any())),
     }
+
+
+def nonequilibrium(rho, psi, ux, uy, mix_tau, solid, prm: OracleParams):
+    """First-order non-equilibrium part of a restart from fields (an extension
+    with no reference counterpart, restating fd_add_nonequilibrium):
+    f_i^(1) = -3 w_i tau_mix Q_i : S(rho u), g_i^(1) = -3 w_i tau Q_i : S(psi u),
+    Q_i = e_i e_i - I/3, S the symmetric part of the gradient by central
+    differences over fluid neighbours (one-sided next to solid cells or
+    lattice edges, zero without a fluid neighbour).  Inputs are full (H, W)
+    arrays; returns (df, dg) of shape (9, H, W), zero on solid cells."""
+    H, W = solid.shape
+    fluid = ~np.asarray(solid, bool)
+    v = np.stack([rho * ux, rho * uy, psi * ux, psi * uy])
+
+    def neighbour(dx, dy):
+        ys, xs = np.mgrid[0:H, 0:W]
+        yy, xx = ys + dy, xs + dx
+        ok = np.ones((H, W), bool)
+        if prm.variant == "walls":
+            ok &= (yy >= 0) & (yy < H)
+        yy = np.mod(yy, H)
+        if prm.variant == "periodic_xy":
+            xx = np.mod(xx, W)
+        else:
+            ok &= (xx >= 0) & (xx < W)
+            xx = np.clip(xx, 0, W - 1)
+        ok &= fluid[yy, xx]
+        return ok, v[:, yy, xx]
+
+    def deriv(dx, dy):
+        okp, vp = neighbour(dx, dy)
+        okm, vm = neighbour(-dx, -dy)
+        return np.where(okp & okm, 0.5 * (vp - vm), np.where(okp, vp - v, np.where(okm, v - vm, 0.0)))
+
+    dxv, dyv = deriv(1, 0), deriv(0, 1)
+    fxx, fyy, fxy = dxv[0], dyv[1], 0.5 * (dyv[0] + dxv[1])
+    gxx, gyy, gxy = dxv[2], dyv[3], 0.5 * (dyv[2] + dxv[3])
+    df = np.zeros((9, H, W))
+    dg = np.zeros((9, H, W))
+    for i in range(9):
+        qxx, qyy, qxy = EX[i] ** 2 - 1 / 3, EY[i] ** 2 - 1 / 3, EX[i] * EY[i]
+        df[i] = -3 * W9[i] * mix_tau * (qxx * fxx + qyy * fyy + 2 * qxy * fxy)
+        dg[i] = -3 * W9[i] * prm.tau * (qxx * gxx + qyy * gyy + 2 * qxy * gxy)
+    df[:, ~fluid] = 0
+    dg[:, ~fluid] = 0
+    return df, dg

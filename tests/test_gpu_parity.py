@@ -415,3 +415,37 @@ def test_fused_matches_oracle_on_random_blocks():
     for k in ("f", "g") + FIELDS:
         assert np.array_equal(got[k], ref[k], equal_nan=k in ("rho", "ux", "uy", "p", "mu", "mix_tau")), \
             (k, _first_diff(got[k], ref[k]))
+
+
+def test_regularised_restart_matches_oracle():
+    """fd_add_nonequilibrium (the regularised restart of restart_from_fields)
+    against the oracle's restatement of the same formula on the same fields,
+    FP64: the populations differ from the equilibrium-only restart by the
+    first-order non-equilibrium part, which carries no density, psi or
+    momentum."""
+    from oracle.lbm_oracle import EX, EY, OracleParams, nonequilibrium
+    fx = load("walls_rects_64x128_500")
+    lat = make_lattice(fx, "f64")
+    lat.step(200)
+    st = lat.state()
+    psi, ux, uy, rho = (np.nan_to_num(st[k]) for k in ("psi", "ux", "uy", "rho"))
+    solid = lat.geometry.solid
+    rho = np.where(solid, 1.0, rho)
+    lat.restart_from_fields(psi, ux, uy, rho=rho)
+    eq = lat.state()
+    lat.restart_from_fields(psi, ux, uy, rho=rho, regularised=True)
+    reg = lat.state()
+    prm = lat.params
+    op = OracleParams(H=prm.H, W=prm.W, variant=prm.variant, tau=prm.tau, eta_n=prm.eta_n, M=prm.M, a=prm.a,
+                      kappa=prm.kappa, gamma=prm.gamma, psi_wall=prm.psi_wall, inlet_ux=prm.inlet_ux,
+                      outlet_coef=prm.outlet_coef)
+    df, dg = nonequilibrium(np.nan_to_num(eq["rho"]), eq["psi"], np.nan_to_num(eq["ux"]), np.nan_to_num(eq["uy"]),
+                            np.nan_to_num(eq["mix_tau"]), solid, op)
+    got_f, got_g = reg["f"] - eq["f"], reg["g"] - eq["g"]
+    assert np.abs(df).max() > 1e-6  # the flow has gradients
+    assert np.allclose(got_f, df, rtol=0, atol=1e-13), np.abs(got_f - df).max()
+    assert np.allclose(got_g, dg, rtol=0, atol=1e-13), np.abs(got_g - dg).max()
+    for d in (got_f, got_g):
+        assert np.abs(d.sum(axis=0)).max() < 1e-15
+        assert np.abs((d * EX[:, None, None]).sum(axis=0)).max() < 1e-15
+        assert np.abs((d * EY[:, None, None]).sum(axis=0)).max() < 1e-15
