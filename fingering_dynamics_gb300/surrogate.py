@@ -662,7 +662,9 @@ def breakthrough_race(net: UNet, members, max_rounds: int, jumps_per_check: int 
     res = {}
     for mode in ("plain", "accelerated"):
         lats = [Lattice(p, g, dtype=dtype) for p, g in members]
-        ens = batch(lats)
+        # the batch puts its lattices into the fused state: the accelerated run builds it after its first
+        # restart (checkpoints and restarts need the reference state)
+        ens = batch(lats) if mode == "plain" else None
         hit_it = [None] * n
         hit_s = [None] * n
         torch.cuda.synchronize()
@@ -685,6 +687,8 @@ def breakthrough_race(net: UNet, members, max_rounds: int, jumps_per_check: int 
                     lat.restart_from_fields(torch.where(lat.fluid, psi, lat.params.psi_wall), ux, uy, rho=lat.rho,
                                             iteration=lat.iteration + jumps_per_check * jump,
                                             regularised=restart == "regularised")
+                if ens is None:
+                    ens = batch(lats)
                 advance(lats, jump, ens)
                 sat_lbm = [float(((lat.psi > 0) & lat.fluid).sum() / lat.fluid.sum().clamp(min=1)) for lat in lats]
                 rejected = [m for m in range(n) if not (np.isfinite(sat_lbm[m]) and abs(sat_lbm[m] - sat_sur[m])
@@ -703,7 +707,8 @@ def breakthrough_race(net: UNet, members, max_rounds: int, jumps_per_check: int 
                     hit_it[m], hit_s[m] = rounds * span, now
             if all(h is not None for h in hit_it):
                 break
-        ens.close()
+        if ens is not None:
+            ens.close()
         res[mode] = {"breakthrough_iteration": hit_it, "breakthrough_s": hit_s, "rounds": rounds}
         del lats
         torch.cuda.empty_cache()
