@@ -25,6 +25,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <type_traits>
 #include <cuda_fp16.h>
 
 #include "fd_common.cuh"
@@ -219,10 +220,24 @@ __device__ __forceinline__ float dev_rcp(float x) {
 template <bool FAST_RCP = false>
 __device__ __forceinline__ DevMacro dev_macros(const DevCoef& c, const float (&d)[9], const DevStencil& st) {
   DevMacro m;
-  m.drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
+  float jx, jy;
+  if constexpr (FAST_RCP) {
+    // 16-bit storage: the sums on direction pairs (1, 2) (3, 4) (5, 6) (7, 8) in packed
+    // FP32x2 arithmetic, as the collision (dev_collide_x2)
+    const float2 d12 = make_float2(d[1], d[2]), d34 = make_float2(d[3], d[4]);
+    const float2 d56 = make_float2(d[5], d[6]), d78 = make_float2(d[7], d[8]);
+    const float2 sp = __fadd2_rn(__fadd2_rn(d12, d34), __fadd2_rn(d56, d78));
+    m.drho = (d[0] + sp.x) + sp.y;
+    const float2 a = __ffma2_rn(d34, make_float2(-1.0f, -1.0f), d12);  // (d1 - d3, d2 - d4)
+    const float2 b = __ffma2_rn(d78, make_float2(-1.0f, -1.0f), d56);  // (d5 - d7, d6 - d8)
+    jx = a.x + (b.x - b.y);
+    jy = a.y + (b.x + b.y);
+  } else {
+    m.drho = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
+    jx = ((d[1] - d[3]) + (d[5] - d[6])) + (d[8] - d[7]);
+    jy = ((d[2] - d[4]) + (d[5] - d[8])) + (d[6] - d[7]);
+  }
   m.rho = 1.0f + m.drho;
-  const float jx = ((d[1] - d[3]) + (d[5] - d[6])) + (d[8] - d[7]);
-  const float jy = ((d[2] - d[4]) + (d[5] - d[8])) + (d[6] - d[7]);
   const float psi = st.psi, gx = st.gx, gy = st.gy;
   m.psi = psi;
   m.gx = gx;
@@ -325,6 +340,99 @@ __device__ __forceinline__ void dev_collide(const DevCoef& c, const DevMacro& m,
   dev_collide_pair<2>(m, a, usq3, ug, omt, omg, d[2], d[4], g[2], g[4]);
   dev_collide_pair<5>(m, b, usq3, ug, omt, omg, d[5], d[7], g[5], g[7]);
   dev_collide_pair<6>(m, b, usq3, ug, omt, omg, d[6], d[8], g[6], g[8]);
+}
+
+// ---- two directions per instruction (16-bit storage) ---------------------------
+// The directions of one weight class pair up with their opposites as (1, 2) |
+// (3, 4) and (5, 6) | (7, 8), so dev_collide_pair<1> and <2> (and <5> and <6>)
+// are one computation on pairs.  dev_collide_x2 does them in the packed FP32x2
+// arithmetic of sm_100-class GPUs (__ffma2_rn, __fadd2_rn, __fmul2_rn: one
+// instruction for both directions, each result rounded as its scalar
+// counterpart), halving the instructions of the eight moving directions; the
+// 16-bit-storage kernels, bound by instruction issue, use it.
+namespace x2 {
+__device__ __forceinline__ float2 sp(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, sp(-1.0f), a); }
+
+struct Class2 {
+  float2 yr, xr, xb, P, gt, gs, gc;
+};
+
+// directions (I, I+1) and their opposites: dp = (d_I, d_I+1), dm = (d_opp I, d_opp I+1)
+__device__ __forceinline__ void collide_set(const Class2& k, float2 t, float2 eg, float2 nusq3, float2 nug, float2 omt,
+                                            float2 omg, float2& dp, float2& dm, float2& gp, float2& gm) {
+  const float2 s2 = fma(t, t, nusq3);
+  const float2 B = fma(eg, t, nug);
+  const float2 Z = fma(k.xr, s2, fma(k.P, B, k.xb));
+  const float2 V = fma(k.yr, t, mul(k.P, eg));
+  dp = fma(omt, dp, add(Z, V));
+  dm = fma(omt, dm, sub(Z, V));
+  const float2 G = fma(k.gs, s2, k.gc);
+  const float2 Gt = mul(k.gt, t);
+  gp = fma(omg, gp, add(G, Gt));
+  gm = fma(omg, gm, sub(G, Gt));
+}
+}  // namespace x2
+
+__device__ __forceinline__ void dev_collide_x2(const DevCoef& c, const DevMacro& m, float (&d)[9], float (&g)[9]) {
+  using namespace x2;
+  const float base = fmaf(3.0f * m.psi, m.mu, m.drho);  // 3p - 1
+  const float ug = m.ux * m.gx + m.uy * m.gy;
+  const float usq3 = 3.0f * (m.ux * m.ux + m.uy * m.uy);
+  float2 g12 = make_float2(g[1], g[2]), g34 = make_float2(g[3], g[4]);
+  float2 g56 = make_float2(g[5], g[6]), g78 = make_float2(g[7], g[8]);
+  const float2 Sp = add(add(g12, g34), add(g56, g78));
+  const float S = Sp.x + Sp.y;
+  const float itg = c.inv_tau_g;
+  {  // rest direction, as dev_collide
+    constexpr float w0 = wgt<0>();
+    const float deq = fmaf(w0, m.drho, fmaf(-0.5f * w0 * m.rho, usq3, -c.c_a0 * m.psi * m.mu));
+    const float F = -(3.0f * w0) * m.pref * ug;
+    d[0] = fmaf(deq - d[0], m.inv_tau, d[0]) + F;
+    const float dg = fmaf(-0.5f * w0 * m.psi, usq3, S - c.c_b0 * m.mu);
+    g[0] = fmaf(dg, itg, g[0]);
+  }
+  Class2 a;  // w = 1/9
+  const float yr = (1.0f / 9.0f) * m.inv_tau * m.rho;
+  a.yr = sp(yr);
+  a.xr = sp(0.5f * yr);
+  a.xb = sp((1.0f / 9.0f) * m.inv_tau * base);
+  a.P = sp((1.0f / 3.0f) * m.pref);
+  const float gt = ((1.0f / 9.0f) * itg) * m.psi;
+  a.gt = sp(gt);
+  a.gs = sp(0.5f * gt);
+  a.gc = sp(((1.0f / 9.0f) * itg) * c.three_gamma * m.mu);
+  Class2 b;  // w = 1/36 = (1/9) / 4
+  b.yr = mul(sp(0.25f), a.yr);
+  b.xr = mul(sp(0.25f), a.xr);
+  b.xb = mul(sp(0.25f), a.xb);
+  b.P = mul(sp(0.25f), a.P);
+  b.gt = mul(sp(0.25f), a.gt);
+  b.gs = mul(sp(0.25f), a.gs);
+  b.gc = mul(sp(0.25f), a.gc);
+  const float2 omt = sp(1.0f - m.inv_tau), omg = sp(1.0f - itg);
+  const float2 nusq3 = sp(-usq3), nug = sp(-ug);
+  float2 d12 = make_float2(d[1], d[2]), d34 = make_float2(d[3], d[4]);
+  float2 d56 = make_float2(d[5], d[6]), d78 = make_float2(d[7], d[8]);
+  // e.u and e.grad psi of directions (1, 2): (u_x, u_y); of (5, 6): (u_x + u_y, u_y - u_x)
+  const float2 u = make_float2(m.ux, m.uy), gr = make_float2(m.gx, m.gy);
+  collide_set(a, mul(sp(3.0f), u), gr, nusq3, nug, omt, omg, d12, d34, g12, g34);
+  const float2 u56 = make_float2(m.ux + m.uy, m.uy - m.ux), g56r = make_float2(m.gx + m.gy, m.gy - m.gx);
+  collide_set(b, mul(sp(3.0f), u56), g56r, nusq3, nug, omt, omg, d56, d78, g56, g78);
+  d[1] = d12.x; d[2] = d12.y; d[3] = d34.x; d[4] = d34.y;
+  d[5] = d56.x; d[6] = d56.y; d[7] = d78.x; d[8] = d78.y;
+  g[1] = g12.x; g[2] = g12.y; g[3] = g34.x; g[4] = g34.y;
+  g[5] = g56.x; g[6] = g56.y; g[7] = g78.x; g[8] = g78.y;
+}
+
+// The collision of the staged kernels: packed pairs for 16-bit storage
+template <typename SF>
+__device__ __forceinline__ void dev_collide_for(const DevCoef& c, const DevMacro& m, float (&d)[9], float (&g)[9]) {
+  if constexpr (!std::is_same_v<SF, float>) dev_collide_x2(c, m, d, g);
+  else dev_collide(c, m, d, g);
 }
 
 // ---- Zou-He on deviations ----------------------------------------------------

@@ -373,9 +373,10 @@ __device__ __forceinline__ float2 psi_cell(const char* sm, const DevArgs<SF>& a,
   if (m & SOLID) return make_float2(a.c.psi_wall, 0.0f);
   if constexpr (psi_paired<SF>()) {
     return dev_psi_pair(g);
-  } else {
-    const float S = ((g[1] + g[2]) + (g[3] + g[4])) + ((g[5] + g[6]) + (g[7] + g[8]));
-    return make_float2(g[0] + S, 0.0f);
+  } else {  // 16-bit storage: the sum on direction pairs in packed FP32x2 arithmetic (dev_collide_x2)
+    const float2 s = __fadd2_rn(__fadd2_rn(make_float2(g[1], g[2]), make_float2(g[3], g[4])),
+                                __fadd2_rn(make_float2(g[5], g[6]), make_float2(g[7], g[8])));
+    return make_float2(g[0] + (s.x + s.y), 0.0f);
   }
 }
 
@@ -535,7 +536,7 @@ __device__ __forceinline__ void tma_strip_ring(const DevArgs<SF>& a, const TmaMa
       if (!(m & SOLID)) {
         const DevMacro mc = dev_macros<!std::is_same_v<SF, float>>(a.c, f, st);
         bad |= nonfinite_cell(mc.rho, mc.psi);
-        dev_collide(a.c, mc, f, gC);
+        dev_collide_for<SF>(a.c, mc, f, gC);
       }
       store_cell<SF, SCALED, STOCH>(a, (size_t)y * a.W + x, f, gC);
     }
@@ -715,7 +716,7 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
       if (!(m & SOLID)) {
         const DevMacro mc = dev_macros<!std::is_same_v<SF, float>>(a.c, f, st);
         bad |= nonfinite_cell(mc.rho, mc.psi);
-        dev_collide(a.c, mc, f, gC);
+        dev_collide_for<SF>(a.c, mc, f, gC);
       }
       store_cell<SF, SCALED, STOCH>(a, (size_t)y * a.W + x, f, gC);
     }
