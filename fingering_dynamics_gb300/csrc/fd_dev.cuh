@@ -244,8 +244,16 @@ __device__ __forceinline__ DevMacro dev_macros(const DevCoef& c, const float (&d
   m.gy = gy;
   m.mu = dev_mu(c, st);  // getMu (fingering_periodic.py:141-144)
   const float inv_rho = dev_rcp<FAST_RCP>(m.rho);
-  m.ux = fmaf(0.5f * m.mu, gx, jx) * inv_rho;             // getUx (fingering_periodic.py:126-132)
-  m.uy = fmaf(0.5f * m.mu, gy, jy) * inv_rho;
+  if constexpr (FAST_RCP) {  // getUx / getUy as one pair
+    const float hm = 0.5f * m.mu;
+    const float2 u = __fmul2_rn(__ffma2_rn(make_float2(hm, hm), make_float2(gx, gy), make_float2(jx, jy)),
+                                make_float2(inv_rho, inv_rho));
+    m.ux = u.x;
+    m.uy = u.y;
+  } else {
+    m.ux = fmaf(0.5f * m.mu, gx, jx) * inv_rho;  // getUx (fingering_periodic.py:126-132)
+    m.uy = fmaf(0.5f * m.mu, gy, jy) * inv_rho;
+  }
   const float rD = m.rho * fmaf(c.eta_diff, psi, c.eta_sum);
   m.inv_tau = rD * dev_rcp<FAST_RCP>(fmaf(0.5f, rD, c.six_eta_prod));  // 1 / getMix_tau
   m.pref = m.mu * fmaf(-0.5f, m.inv_tau, 1.0f);              // mu (1 - 1/(2 tau))
