@@ -46,6 +46,13 @@
 #ifndef FD_TMA_NS_16
 #define FD_TMA_NS_16 5
 #endif
+// 1: the split ring walks odd strips from their top row down, so neighbouring
+// strips (handed out close together by the single-lattice grid and by the
+// batch's tile table) read their shared halo rows at about the same time;
+// 0: every strip walks up.  Same results either way.
+#ifndef FD_TMA_WALK_DOWN
+#define FD_TMA_WALK_DOWN 1
+#endif
 
 namespace fd {
 
@@ -598,12 +605,20 @@ __device__ __forceinline__ float inlet_corner_drho(const DevArgs<SF>& a, int yn)
 // refilled as soon as it is no longer read: the g half of row y+4 and the f
 // half of row y+2 are issued at the barrier of row y, 1.5 and 1 rows ahead of
 // their first use.  The mask row of r (needed up to the f pull of row r)
-// arrives with the g half into mask-ring row (r - first) & 7.  The f half of
+// arrives with the g half into mask-ring row (r - first) % 6.  The f half of
 // row y0-2 is never needed (the inlet corners read global memory), so the
 // prologue fills f rows y0-1 .. y0+2.
+//
+// `down` walks the strip from its top row to its bottom row instead: the
+// ring schedule is the same in the strip's own row order (local row l is
+// lattice row y0 + l going up, y1 - 1 - l going down), and the cell update
+// takes its rows and psi values in lattice order, so the results are the same
+// bit for bit.  Odd strips walk down (FD_TMA_WALK_DOWN): the two strips that
+// share a boundary then read its halo rows at about the same time (both at
+// their start, or both at their end) and the second read finds them in L2.
 template <typename SF, int NT, bool SCALED, bool STOCH>
 __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaMaps* tm, int band, int strip,
-                                                char* smem, unsigned& phase, bool& ok) {
+                                                bool down, char* smem, unsigned& phase, bool& ok) {
   using L = SlotLayout<SF, NT>;
   using M = TmaSmem<SF, NT, 4>;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + M::OFF_BAR);
@@ -613,96 +628,109 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
   const int t = threadIdx.x;
   const int x0 = band * NT;
   const int y0 = strip * a.R, y1 = min(y0 + a.R, a.H);
+  const int n = y1 - y0;  // local rows -2 .. n+1: g halves -2 .. n+1, f halves -1 .. n
   const int x = x0 + t;
   const bool owned = x < a.W;
   const bool walls = a.variant == FD_VARIANT_WALLS;
-  const int first = y0 - 2, last = y1 + 1;  // g rows y0-2 .. y1+1, f rows y0-1 .. y1
   const int hl = (t == NT / 2) ? -1 : (t == NT - 1 ? NT : 0);
   const bool halo = (t == NT / 2) || (t == NT - 1);
 
-  auto slot = [&](int r) { return M::OFF_SLOT + ((r - first) & 3) * M::SLOT; };
-  auto mrow = [&](int r) { return M::OFF_MASK + (int)((unsigned)(r - first) % (unsigned)M::MASK_ROWS) * L::RM; };
+  auto lat = [&](int l) { return down ? y1 - 1 - l : y0 + l; };  // lattice row of local row l
+  auto slot = [&](int l) { return M::OFF_SLOT + ((l + 2) & 3) * M::SLOT; };
+  auto mrow = [&](int l) { return M::OFF_MASK + (int)((unsigned)(l + 2) % (unsigned)M::MASK_ROWS) * L::RM; };
+  // slots of the lattice rows below, at and above local row l
+  auto rows_of = [&](int l, int (&rows)[3]) {
+    rows[0] = slot(down ? l + 1 : l - 1);
+    rows[1] = slot(l);
+    rows[2] = slot(down ? l - 1 : l + 1);
+  };
   // parity bits of the fills issued (thread 0), for the error path
   unsigned issued = phase;
-  auto issue_g = [&](int r) {
-    if (r > last || !ok) return;
-    const int b = (r - first) & 3;
-    issue_g_half<SF, NT>(a, tm, smem + slot(r), smem + mrow(r), &bars[b], r, x0);
+  auto issue_g = [&](int l) {
+    if (l > n + 1 || !ok) return;
+    const int b = (l + 2) & 3;
+    issue_g_half<SF, NT>(a, tm, smem + slot(l), smem + mrow(l), &bars[b], lat(l), x0);
     issued ^= 1u << b;
   };
-  auto issue_f = [&](int r) {
-    if (r > y1 || !ok) return;
-    const int b = 4 + ((r - first) & 3);
-    issue_f_half<SF, NT>(a, tm, smem + slot(r), &bars[b], r, x0);
+  auto issue_f = [&](int l) {
+    if (l > n || !ok) return;
+    const int b = 4 + ((l + 2) & 3);
+    issue_f_half<SF, NT>(a, tm, smem + slot(l), &bars[b], lat(l), x0);
     issued ^= 1u << b;
   };
   auto wait_bar = [&](int b) {
     if (ok) ok = mbar_wait(&bars[b], (phase >> b) & 1u);
     phase ^= 1u << b;
   };
-  auto wait_g = [&](int r) { wait_bar((r - first) & 3); };
-  auto wait_f = [&](int r) { wait_bar(4 + ((r - first) & 3)); };
+  auto wait_g = [&](int l) { wait_bar((l + 2) & 3); };
+  auto wait_f = [&](int l) { wait_bar(4 + ((l + 2) & 3)); };
 
   if (t == 0) {
-    for (int r = first; r < first + 4; ++r) issue_g(r);
-    for (int r = y0 - 1; r < y0 + 3; ++r) issue_f(r);
+    for (int l = -2; l < 2; ++l) issue_g(l);
+    for (int l = -1; l < 3; ++l) issue_f(l);
   }
-  int pslot = 0;  // psi ring slot of row y0-1; rows y0-1, y0, y0+1 use pslot, +1, +2 (mod 4)
+  int pslot = 0;  // psi ring slot of local row -1; local rows -1, 0, 1 use pslot, +1, +2 (mod 4)
   auto psi_row = [&](int k) { return ((pslot + k) & 3) * M::PSI_ROW; };
-  // psi of ring row r (this thread's cell and its halo cell) into psi ring row k
+  // psi of local row l (this thread's cell and its halo cell) into psi ring row k
   float gN[9];
-  auto psi_of_row = [&](int r, int k) {
-    const int rows[3] = {slot(r - 1), slot(r), slot(r + 1)};
+  auto psi_of_row = [&](int l, int k) {
+    int rows[3];
+    rows_of(l, rows);
+    const int r = lat(l);
     const bool ghost = walls && (r < 0 || r >= a.H);
     const int yr = wrap(r, a.H);
     const int pr = psi_row(k);
-    const float2 pv = ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(r), x, t, yr, gN);
+    const float2 pv = ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(l), x, t, yr, gN);
     ring.put(pr, t + 1, pv);
     if (halo) {
       float gh[9];
-      ring.put(pr, hl + 1, ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(r), x0 + hl, hl, yr, gh));
+      ring.put(pr, hl + 1, ghost ? wallv : psi_cell<SF, NT, SCALED>(smem, a, rows, mrow(l), x0 + hl, hl, yr, gh));
     }
     return pv;
   };
 
-  // prologue: psi of rows y0-1 and y0; the g halves of rows y0-2 and y0-1
-  // are refilled (rows y0+2, y0+3) as soon as each is done
-  wait_g(y0 - 2);
-  wait_g(y0 - 1);
-  wait_g(y0);
-  float2 pS = psi_of_row(y0 - 1, 0);  // psi of this column at rows y-1 and y
-  bool bad = false;                   // a fluid cell with a non-finite rho or psi
+  // prologue: psi of local rows -1 and 0; the g halves of local rows -2 and
+  // -1 are refilled (local rows 2, 3) as soon as each is done
+  wait_g(-2);
+  wait_g(-1);
+  wait_g(0);
+  float2 pP = psi_of_row(-1, 0);  // psi of this column at local rows l-1 and l
+  bool bad = false;               // a fluid cell with a non-finite rho or psi
   __syncthreads();
-  if (t == 0) issue_g(y0 + 2);
-  wait_g(y0 + 1);
-  float2 pC = psi_of_row(y0, 1);
+  if (t == 0) issue_g(2);
+  wait_g(1);
+  float2 pC = psi_of_row(0, 1);
   float gC[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) gC[i] = gN[i];
   __syncthreads();
-  if (t == 0) issue_g(y0 + 3);
-  wait_f(y0 - 1);
-  wait_f(y0);
+  if (t == 0) issue_g(3);
+  wait_f(-1);
+  wait_f(0);
 
-  for (int y = y0; y < y1; ++y) {
-    // 1. psi of row y+1 from the g halves of rows y, y+1, y+2
-    wait_g(y + 2);
-    const float2 pN = psi_of_row(y + 1, 2);
+  for (int l = 0; l < n; ++l) {
+    const int y = lat(l);
+    // 1. psi of local row l+1 from the g halves of local rows l, l+1, l+2
+    wait_g(l + 2);
+    const float2 pX = psi_of_row(l + 1, 2);
     float drho_nb = 0.0f;
     if (walls && x == 0 && (y == 0 || y == a.H - 1)) drho_nb = inlet_corner_drho<SF, SCALED>(a, y == 0 ? 1 : a.H - 2);
-    // 2. psi(y+1) complete: the g half of row y and the f half of row y-2 are
-    //    free (the f half of row y0+2 was filled by the prologue)
+    // 2. psi(l+1) complete: the g half of local row l and the f half of local
+    //    row l-2 are free (the f half of local row 2 was filled by the prologue)
     __syncthreads();
     if (t == 0) {
-      issue_g(y + 4);
-      if (y > y0) issue_f(y + 2);
+      issue_g(l + 4);
+      if (l > 0) issue_f(l + 2);
     }
-    wait_f(y + 1);
-    // 3. stencils, f pull, Zou-He, collision, store
+    wait_f(l + 1);
+    // 3. stencils, f pull, Zou-He, collision, store (rows and psi in lattice order)
     if (owned) {
-      const DevStencil st = ring_stencil(ring, psi_row(0), psi_row(1), psi_row(2), t + 1, pS, pC, pN);
-      const int rows[3] = {slot(y - 1), slot(y), slot(y + 1)};
-      const unsigned m = mask_at<SF, NT>(smem, mrow(y), t);
+      const float2 pS = down ? pX : pP, pN = down ? pP : pX;
+      const DevStencil st = ring_stencil(ring, psi_row(down ? 2 : 0), psi_row(1), psi_row(down ? 0 : 2), t + 1, pS,
+                                         pC, pN);
+      int rows[3];
+      rows_of(l, rows);
+      const unsigned m = mask_at<SF, NT>(smem, mrow(l), t);
       float f[9];
       pull_cell<SF, NT, false, SCALED>(smem, a.c, rows, t, m & 0xFFu, f);
       if (x == 0 || x == a.W - 1) {
@@ -722,8 +750,8 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) gC[i] = gN[i];
-    pS = pC;
-    pC = pN;
+    pP = pC;
+    pC = pX;
     pslot = (pslot + 1) & 3;
   }
   // After a wait gave up no further copies were issued; make sure the last
@@ -736,10 +764,12 @@ __device__ __forceinline__ void tma_strip_split(const DevArgs<SF>& a, const TmaM
   ok = __syncthreads_and(ok);
 }
 
+// `down`: walk the strip from its top row (the split ring only; the
+// whole-row ring always walks up).
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
-__device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, const TmaMaps* tm, int band, int strip, char* smem,
-                                          unsigned& phase, bool& ok) {
-  if constexpr (NS == 4) tma_strip_split<SF, NT, SCALED, STOCH>(a, tm, band, strip, smem, phase, ok);
+__device__ __forceinline__ void tma_strip(const DevArgs<SF>& a, const TmaMaps* tm, int band, int strip, bool down,
+                                          char* smem, unsigned& phase, bool& ok) {
+  if constexpr (NS == 4) tma_strip_split<SF, NT, SCALED, STOCH>(a, tm, band, strip, down, smem, phase, ok);
   else tma_strip_ring<SF, NT, NS, SCALED, STOCH>(a, tm, band, strip, smem, phase, ok);
 }
 
@@ -768,9 +798,8 @@ constexpr int tma_resident_ctas() {
 static_assert(FD_TMA_NS_F32 != 4 || tma_resident_ctas<float, 128, 4>() >= 5,
               "the FP32 split ring must fit five CTAs per SM");
 
-// CTA b takes band b % nbands of strip strip0 + b / nbands.  `tm`: the tensor
-// maps of the step's source planes (a grid constant: TMA reads it from the
-// parameter space).
+// CTA b takes band b % nbands of strip strip0 + b / nbands.  `tm`: the tensor maps of the step's source planes
+// (a grid constant: TMA reads it from the parameter space).
 template <typename SF, int NT, int NS, bool SCALED, bool STOCH>
 __global__ void __launch_bounds__(NT) k_fused_tma(const __grid_constant__ DevArgs<SF> a, int nbands, int strip0,
                                                   const __grid_constant__ TmaMaps tm) {
@@ -779,8 +808,9 @@ __global__ void __launch_bounds__(NT) k_fused_tma(const __grid_constant__ DevArg
   init_ring<SF, NT, NS>(smem);
   unsigned phase = 0;
   bool ok = true;
-  tma_strip<SF, NT, NS, SCALED, STOCH>(a, &tm, (int)blockIdx.x % nbands, strip0 + (int)blockIdx.x / nbands, smem,
-                                       phase, ok);
+  const int strip = strip0 + (int)blockIdx.x / nbands;
+  tma_strip<SF, NT, NS, SCALED, STOCH>(a, &tm, (int)blockIdx.x % nbands, strip, FD_TMA_WALK_DOWN && (strip & 1),
+                                       smem, phase, ok);
 }
 
 // One lattice of a batch: its arguments and the tensor maps of its source
@@ -843,7 +873,7 @@ __global__ void __launch_bounds__(NT, (NS == 4 ? tma_resident_ctas<SF, NT, NS>()
       continue;
     }
     const int4 tl = tiles[k];
-    tma_strip<SF, NT, NS, SCALED, STOCH>(sa, stm, tl.y, tl.z, smem, phase, ok);
+    tma_strip<SF, NT, NS, SCALED, STOCH>(sa, stm, tl.y, tl.z, FD_TMA_WALK_DOWN && (tl.z & 1), smem, phase, ok);
   }
 }
 
