@@ -46,10 +46,13 @@
 #ifndef FD_TMA_NS_16
 #define FD_TMA_NS_16 5
 #endif
-// 1: the split ring walks odd strips from their top row down, so neighbouring
-// strips (handed out close together by the single-lattice grid and by the
-// batch's tile table) read their shared halo rows at about the same time;
-// 0: every strip walks up.  Same results either way.
+// 1: the single-lattice kernel walks the odd strips of the split ring from
+// their top row down, so neighbouring strips (launched close together) read
+// their shared halo rows at about the same time; 0: every strip walks up.
+// Same results either way.  The batch kernel always walks up: its tiles come
+// from a counter, largest first, and walking down measured 1.9% slower on the
+// 96-member ensemble (36,188 vs 36,874 MLUPS) while the single lattice gains
+// 0.6% (DRAM reads 694 -> 630 MB per launch on 4096 x 2048).
 #ifndef FD_TMA_WALK_DOWN
 #define FD_TMA_WALK_DOWN 1
 #endif
@@ -873,7 +876,7 @@ __global__ void __launch_bounds__(NT, (NS == 4 ? tma_resident_ctas<SF, NT, NS>()
       continue;
     }
     const int4 tl = tiles[k];
-    tma_strip<SF, NT, NS, SCALED, STOCH>(sa, stm, tl.y, tl.z, FD_TMA_WALK_DOWN && (tl.z & 1), smem, phase, ok);
+    tma_strip<SF, NT, NS, SCALED, STOCH>(sa, stm, tl.y, tl.z, false, smem, phase, ok);
   }
 }
 
