@@ -688,7 +688,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--dtype", default="f32", choices=sorted(BYTES_PER_LU))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--rows", type=int, default=0, help="rows per warp (0 = automatic)")
+    ap.add_argument("--rows", type=int, default=0,
+                    help="strip height of the staged kernel, rows per warp of the others (0 = automatic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end measurement")
     ap.add_argument("--no-extras", action="store_true",

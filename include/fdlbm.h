@@ -262,7 +262,9 @@ int fd_unpack(const fd_params* prm, const fd_storage* st, const void* src, int d
 /* fd_fused_step on packed buffers (the same loop body, fingering_periodic.py:454-479
  * / fingering.py:558-585, computed in FP32 in deviation form).  pop_a/pop_b:
  * fd_packed_bytes() each, 256-byte aligned; side_a/side_b: 6*H floats.
- * W must be a multiple of 4. */
+ * W must be a multiple of 4.  rows_per_warp: for W a multiple of 8 the strip
+ * height in rows of the staged kernel (one CTA per band of 128 cells and strip),
+ * otherwise the rows one warp of the register kernel marches; 0 = automatic. */
 int fd_fused_step_packed(const fd_params* prm, const fd_storage* st, const uint16_t* mask, const double* inlet_ux,
                          void* pop_a, void* pop_b, void* side_a, void* side_b, int nsteps, int rows_per_warp,
                          void* stream);
