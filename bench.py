@@ -644,8 +644,9 @@ def run_surrogate(args):
 
 def run_convs(args):
     """Every convolution shape of the surrogate's training step (forward and
-    data gradient, batch `--batch` at 512 x 256): the warp-level and the
-    tcgen05 kernel timed with CUDA events, one JSON line per shape."""
+    data gradient, batch `--batch` at 512 x 256): the warp-level, the tcgen05
+    and (widths that are multiples of 128) the TMA-fed tcgen05 kernel timed
+    with CUDA events, one JSON line per shape."""
     import ctypes as C
     import torch
     from fingering_dynamics_gb300 import _lib as L
@@ -666,7 +667,9 @@ def run_convs(args):
         z = torch.empty_like(y)
         fl = 2.0 * 9 * ci * co * N * H * W
         line = {"metric": "conv3x3 throughput", "unit": "TFLOP/s", "shape": [N, H, W, ci, co]}
-        for fn, key in (("sg_conv3x3", "mma"), ("sg_conv3x3_tc", "tcgen05")):
+        for fn, key in (("sg_conv3x3", "mma"), ("sg_conv3x3_tc", "tcgen05"), ("sg_conv3x3_tma", "tma")):
+            if key == "tma" and W % 128:
+                continue
             for _ in range(args.warmup):
                 L.call(fn, p(x), N, H, W, ci, p(w), None, co, 1, p(z), p(y), None)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -18,6 +18,13 @@
 // with tcgen05.ld (each warp its 32 lanes = 32 pixels), adds the bias,
 // applies GELU and stores bfloat16.
 //
+// The TMA-fed variant (k_conv3x3_tma, sg_conv3x3_tma) keeps the halo tiles'
+// shared-memory layout but fills it with tensor-map boxes issued by one
+// thread into a ring of stages completing on mbarriers (zero fill outside
+// the image is the convolution's padding), and the same thread issues the
+// MMAs as soon as a stage has landed: no thread copies operands and no CTA
+// barrier separates the chunks.
+//
 // Every mbarrier wait is bounded; a wait that gives up sets bit 0 of
 // g_sg_tc_error (read by sg_tc_status) and the kernel continues without
 // hanging; TMEM is always released.
@@ -27,6 +34,7 @@
 
 #include "../../include/fdsurrogate.h"
 #include "fd_host.h"
+#include "fd_tmap.h"
 
 namespace sg {
 
@@ -71,6 +79,51 @@ __device__ __forceinline__ void mbar_wait(uint64_t* bar, unsigned parity) {
     if (done) return;
   }
   atomicOr(&g_sg_tc_error, 1u);
+}
+
+// bounded wait that reports whether the phase completed.  `bail`: also give
+// up once any wait of the launch has given up (the error word is set), so a
+// failure common to every CTA does not cost every CTA a wait's full limit;
+// the waits that drain copies and MMAs in flight before a CTA exits keep the
+// full limit.
+__device__ __forceinline__ bool mbar_wait_ok(uint64_t* bar, unsigned parity, bool bail) {
+  const uint32_t a = smem_u32(bar);
+  for (unsigned it = 0; it < kTcWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (bail && (it & 1023u) == 1023u && *reinterpret_cast<volatile unsigned*>(&g_sg_tc_error) != 0u) return false;
+  }
+  atomicOr(&g_sg_tc_error, 1u);
+  return false;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// one box of a 3-D / 4-D tensor map into shared memory (128-byte aligned
+// destination; the innermost coordinate times the element size a multiple of
+// 16 bytes)
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
 }
 
 // shared-memory matrix descriptor: canonical K-major layout, no swizzle
@@ -452,6 +505,285 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tch(const bf16* __restri
   }
 }
 
+// ---------------------------------------------------------------------------
+// TMA-fed halo tiles.  A CTA owns R image rows x 128 pixels x BN output
+// channels (R accumulators of BN TMEM columns); K advances in chunks of 16
+// input channels, each chunk one stage of the ring:
+//   A: two boxes (8 channels x 130 pixels x R+2 rows of one image) of the 4-D
+//      map (C, W, H, N) over x, landing as [row][pixel][8 channels] = the
+//      halo kernel's row blocks (16 B per pixel, SBO 128 B), the second
+//      K-slice SLICE bytes after the first (LBO); out-of-image pixels and rows
+//      read as zero, the convolution's padding;
+//   B: one box (8 channels x 1 tap x BN output channels) of the 3-D map
+//      (Cin, 9, Cout) over the weights per tap and K-slice, landing as BN rows
+//      of 16 B (SBO 128 B), the second K-slice BN x 16 B after the first (LBO).
+// Thread 0 issues the boxes of S chunks ahead, waits for a stage to land,
+// issues its 9 x R MMAs and commits them to the stage's second mbarrier; the
+// stage of the previous chunk is refilled once its MMAs have completed, so
+// the MMAs of a chunk are queued while that wait runs.  The other threads
+// wait at the CTA barrier before the epilogue.
+// ---------------------------------------------------------------------------
+struct ConvMaps {
+  CUtensorMap x, w;
+};
+
+template <int BN, int R, int S>
+struct TmaConvCfg {
+  static constexpr int A_BOX = (R + 2) * kHaloPx * 16;      // bytes of one A box
+  static constexpr int SLICE = (A_BOX + 127) / 128 * 128;   // one 8-channel slice of the halo
+  static constexpr int ROWB = kHaloPx * 16;                 // one input row of a slice
+  static constexpr int A_BYTES = 2 * SLICE;
+  static constexpr int BSL = BN * 16;                       // one tap's K-slice of weights
+  static constexpr int TB = 2 * BSL;                        // one tap's weights
+  static constexpr int STAGE = A_BYTES + 9 * TB;
+  static constexpr int TX = 2 * A_BOX + 18 * BSL;           // bytes the boxes of a stage bring
+  static constexpr int OFF_BAR = S * STAGE;
+  static constexpr int SMEM = OFF_BAR + 2 * S * 8 + 16 + 128;  // + mbarriers, TMEM address, alignment
+  static constexpr int NCOL = R * BN;
+  static constexpr int COLS = NCOL <= 32 ? 32 : (NCOL <= 64 ? 64 : (NCOL <= 128 ? 128 : (NCOL <= 256 ? 256 : 512)));
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256 && NCOL <= 512, "tile");
+  static_assert(STAGE % 128 == 0 && SLICE % 128 == 0 && BSL % 128 == 0, "128-byte aligned box destinations");
+};
+
+// shared memory of TmaConvCfg<BN, R, S> (the stage count that fits is chosen
+// before the configuration is instantiated)
+constexpr int tma_conv_smem(int BN, int R, int S) {
+  return S * (2 * (((R + 2) * kHaloPx * 16 + 127) / 128 * 128) + 18 * BN * 16) + 2 * S * 8 + 16 + 128;
+}
+
+template <int BN, int R, int S>
+__global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tma(const __grid_constant__ ConvMaps maps, int H,
+                                                              int W, int Cin, const float* __restrict__ bias,
+                                                              int Cout, int act, bf16* __restrict__ z,
+                                                              bf16* __restrict__ y) {
+  using C = TmaConvCfg<BN, R, S>;
+  extern __shared__ char smem_raw[];
+  char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+  uint64_t* empty = full + S;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(empty + S);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tiles_x = W / kTcBM;
+  const int tx = blockIdx.x % tiles_x, rblk = blockIdx.x / tiles_x;
+  const int row = rblk * R;  // first output row = n * H + yy (H % R == 0)
+  const int n = row / H, yy = row % H;
+  const int x0 = tx * kTcBM;
+  const int co0 = blockIdx.y * BN;
+  const int nk = Cin / 16;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(C::COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 2 * S; ++i) mbar_init(&full[i]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (tid == 0) {
+    // chunk whose boxes / MMAs are in flight on each stage and not yet waited for (-1: none)
+    int pend_full[S], pend_empty[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) pend_full[i] = pend_empty[i] = -1;
+    auto issue = [&](int kc, int st) {
+      char* As = smem + st * C::STAGE;
+      char* Bs = As + C::A_BYTES;
+      mbar_expect_tx(&full[st], (unsigned)C::TX);
+#pragma unroll
+      for (int s = 0; s < 2; ++s) tma_load_4d(As + s * C::SLICE, &maps.x, kc * 16 + 8 * s, x0 - 1, yy - 1, n, &full[st]);
+#pragma unroll
+      for (int tap = 0; tap < 9; ++tap)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) tma_load_3d(Bs + tap * C::TB + s * C::BSL, &maps.w, kc * 16 + 8 * s, tap, co0, &full[st]);
+      pend_full[st] = kc;
+    };
+    constexpr uint32_t idesc = instr_desc<kTcBM, BN>();
+    bool ok = true;
+    for (int c = 0; c < S && c < nk; ++c) issue(c, c);
+    for (int kc = 0; kc < nk && ok; ++kc) {
+      const int st = kc % S;
+      ok = mbar_wait_ok(&full[st], (unsigned)(kc / S) & 1u, true);
+      if (!ok) break;
+      pend_full[st] = -1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = smem_u32(smem + st * C::STAGE), b0 = a0 + C::A_BYTES;
+#pragma unroll
+      for (int tap = 0; tap < 9; ++tap) {
+        const int ky = tap / 3, kx = tap % 3;
+        const uint64_t bd = smem_desc(b0 + tap * C::TB, C::BSL, 128);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const uint64_t ad = smem_desc(a0 + (r + ky) * C::ROWB + kx * 16, C::SLICE, 128);
+          tc_mma(tmem + (uint32_t)(r * BN), ad, bd, idesc, (kc > 0 || tap > 0) ? 1u : 0u);
+        }
+      }
+      tc_commit(&empty[st]);
+      pend_empty[st] = kc;
+      // refill the stage of chunk kc-1 once its MMAs have completed
+      if (kc >= 1 && kc - 1 + S < nk) {
+        const int ps = (kc - 1) % S;
+        ok = mbar_wait_ok(&empty[ps], (unsigned)((kc - 1) / S) & 1u, true);
+        if (!ok) break;
+        pend_empty[ps] = -1;
+        issue(kc - 1 + S, ps);
+      }
+    }
+    // every box and MMA issued has completed (bounded waits) before the
+    // accumulators are read, the shared memory is released or TMEM freed
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      if (pend_full[i] >= 0) mbar_wait_ok(&full[i], (unsigned)(pend_full[i] / S) & 1u, false);
+      if (pend_empty[i] >= 0) mbar_wait_ok(&empty[i], (unsigned)(pend_empty[i] / S) & 1u, false);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+#pragma unroll 1
+  for (int r = 0; r < R; ++r) {
+    const long long p = ((long long)(row + r) * W + x0) + warp * 32 + lane;
+#pragma unroll
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(r * BN + c0), v);
+      const int co = co0 + c0;
+      uint32_t zw[8], yw[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        float t0 = v[2 * i] + (bias ? bias[co + 2 * i] : 0.0f);
+        float t1 = v[2 * i + 1] + (bias ? bias[co + 2 * i + 1] : 0.0f);
+        const __nv_bfloat162 zp = __floats2bfloat162_rn(t0, t1);
+        zw[i] = *reinterpret_cast<const uint32_t*>(&zp);
+        if (act == SG_ACT_GELU) {
+          t0 = gelu_f(t0);
+          t1 = gelu_f(t1);
+        }
+        const __nv_bfloat162 yp = __floats2bfloat162_rn(t0, t1);
+        yw[i] = *reinterpret_cast<const uint32_t*>(&yp);
+      }
+      const size_t o = (size_t)p * Cout + co;
+      if (z) {
+        reinterpret_cast<uint4*>(z + o)[0] = make_uint4(zw[0], zw[1], zw[2], zw[3]);
+        reinterpret_cast<uint4*>(z + o)[1] = make_uint4(zw[4], zw[5], zw[6], zw[7]);
+      }
+      if (y) {
+        reinterpret_cast<uint4*>(y + o)[0] = make_uint4(yw[0], yw[1], yw[2], yw[3]);
+        reinterpret_cast<uint4*>(y + o)[1] = make_uint4(yw[4], yw[5], yw[6], yw[7]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::COLS) : "memory");
+  }
+}
+
+// Tensor maps of one call: x as (C, W, H, N) with boxes of 8 channels x 130
+// pixels x R+2 rows, the weights [co][tap][ci] as (Cin, 9, Cout) with boxes of
+// 8 channels x 1 tap x BN output channels.
+inline int encode_conv_maps(ConvMaps& m, const bf16* x, int N, int H, int W, int Cin, const bf16* w, int Cout,
+                            int R, int BN) {
+  const fd::EncodeTiledFn fn = fd::encode_tiled_fn();
+  FD_REQUIRE(fn != nullptr, FD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const cuuint64_t es = 2;
+  const cuuint64_t xd[4] = {(cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+  const cuuint64_t xs[3] = {Cin * es, (cuuint64_t)W * Cin * es, (cuuint64_t)H * W * Cin * es};
+  const cuuint32_t xb[4] = {8u, (cuuint32_t)kHaloPx, (cuuint32_t)(R + 2), 1u};
+  const cuuint32_t e4[4] = {1u, 1u, 1u, 1u};
+  CUresult r = fn(&m.x, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(x), xd, xs, xb, e4,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  FD_REQUIRE(r == CUDA_SUCCESS, FD_ERR_CUDA, "sg_conv3x3_tma: input tensor map (%d)", (int)r);
+  const cuuint64_t wd[3] = {(cuuint64_t)Cin, 9u, (cuuint64_t)Cout};
+  const cuuint64_t ws[2] = {Cin * es, 9u * Cin * es};
+  const cuuint32_t wb[3] = {8u, 1u, (cuuint32_t)BN};
+  r = fn(&m.w, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16*>(w), wd, ws, wb, e4,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  FD_REQUIRE(r == CUDA_SUCCESS, FD_ERR_CUDA, "sg_conv3x3_tma: weight tensor map (%d)", (int)r);
+  return FD_OK;
+}
+
+#ifndef SG_TMA_PAIR
+#define SG_TMA_PAIR 1
+#endif
+constexpr int kSmPerSmBytes = 233472;  // shared memory of an SM (228 KB), 1 KB of it reserved per CTA
+
+template <int BN, int R, int S>
+int launch_tma_r(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
+                 bf16* z, bf16* y, cudaStream_t s) {
+  using C = TmaConvCfg<BN, R, S>;
+  static_assert(C::SMEM <= 227 * 1024 && C::SMEM == tma_conv_smem(BN, R, S), "shared memory");
+  auto kern = k_conv3x3_tma<BN, R, S>;
+  static std::atomic<unsigned long long> attr_done{0};
+  if (fd::ensure_smem_attr(kern, 227 * 1024, attr_done) != cudaSuccess)
+    return fd::check_launch("sg_conv3x3_tma: shared-memory attribute");
+  // no more CTAs per SM than their tensor memory columns fit (512): a larger
+  // shared-memory request keeps the others off the SM instead of blocking in
+  // tcgen05.alloc
+  int smem = C::SMEM;
+  const int fit = 512 / C::COLS;
+  if (kSmPerSmBytes / (smem + 1024) > fit) smem = kSmPerSmBytes / (fit + 1) - 1024 + 1;
+  if (smem > 227 * 1024) smem = 227 * 1024;
+  ConvMaps maps;
+  if (int r = encode_conv_maps(maps, x, N, H, W, Cin, w, Cout, R, BN)) return r;
+  dim3 grid((unsigned)((long long)N * (H / R) * (W / kTcBM)), (unsigned)(Cout / BN));
+  kern<<<grid, kTcThreads, smem, s>>>(maps, H, W, Cin, b, Cout, act, z, y);
+  return fd::check_launch("sg_conv3x3_tma");
+}
+
+// Tiles of at most 64 output channels are paired (with SG_TMA_PAIR): two CTAs
+// share an SM, one's epilogue running while the other multiplies (measured
+// on the surrogate's layers: 64 -> 64 channels 346 vs 283 TFLOP/s, 96 -> 32
+// 293 vs 222); 128-channel tiles keep one CTA with four rows (two CTAs of
+// 128 x 4 accumulators would not fit the tensor memory, and two rows lose:
+// 384 -> 128 channels 524 vs 612 TFLOP/s).
+template <int BN>
+constexpr bool tma_paired() {
+  return SG_TMA_PAIR && BN <= 64;
+}
+
+// Stages: one for a single chunk; two or three where paired CTAs fit an SM,
+// else as many as fit one CTA (up to four).
+template <int BN, int R>
+int launch_tma_s(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
+                 bf16* z, bf16* y, cudaStream_t s) {
+  const int nk = Cin / 16;
+  if (nk == 1) return launch_tma_r<BN, R, 1>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  constexpr int pair = kSmPerSmBytes / 2 - 1024;
+  if constexpr (tma_paired<BN>() && tma_conv_smem(BN, R, 2) <= pair) {
+    if constexpr (tma_conv_smem(BN, R, 3) <= pair) {
+      if (nk >= 3) return launch_tma_r<BN, R, 3>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+    }
+    return launch_tma_r<BN, R, 2>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  } else {
+    if constexpr (tma_conv_smem(BN, R, 4) <= 227 * 1024) {
+      if (nk >= 4) return launch_tma_r<BN, R, 4>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+    }
+    if constexpr (tma_conv_smem(BN, R, 3) <= 227 * 1024) {
+      if (nk >= 3) return launch_tma_r<BN, R, 3>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+    }
+    return launch_tma_r<BN, R, 2>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  }
+}
+
+// rows per CTA: four where the height allows, else two or one
+template <int BN>
+int launch_tma(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
+               bf16* z, bf16* y, cudaStream_t s) {
+  if (H % 4 == 0) return launch_tma_s<BN, 4>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  if (H % 2 == 0) return launch_tma_s<BN, 2>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  return launch_tma_s<BN, 1>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+}
+
 template <int BN, int BK, int R>
 int launch_tch_r(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
                  bf16* z, bf16* y, cudaStream_t s) {
@@ -527,6 +859,25 @@ int sg_conv3x3_tc(const void* x, int N, int H, int W, int Cin, const void* w, co
   if (Cin % 64 == 0) return sg::tc_bk<64>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
   if (Cin % 32 == 0) return sg::tc_bk<32>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
   return sg::tc_bk<16>(xb, N, H, W, Cin, wb, bias, Cout, act, (bf16*)z, (bf16*)y, s);
+}
+
+int sg_conv3x3_tma(const void* x, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout,
+                   int act, void* z, void* y, void* stream) {
+  FD_REQUIRE(x && w && (z || y) && N > 0 && H > 0 && W > 0, FD_ERR_ARG, "sg_conv3x3_tma: bad arguments");
+  FD_REQUIRE(W % sg::kTcBM == 0 && Cin % 16 == 0 && Cout % 16 == 0 && Cin > 0 && Cout > 0, FD_ERR_SHAPE,
+             "sg_conv3x3_tma: needs W a multiple of 128 and channel counts multiples of 16 (got W=%d, %d -> %d)", W,
+             Cin, Cout);
+  FD_REQUIRE(act == SG_ACT_NONE || act == SG_ACT_GELU, FD_ERR_ARG, "sg_conv3x3_tma: activation %d", act);
+  FD_REQUIRE(((uintptr_t)x | (uintptr_t)w | (uintptr_t)z | (uintptr_t)y) % 16 == 0, FD_ERR_ARG,
+             "sg_conv3x3_tma: tensors must be 16-byte aligned");
+  using sg::bf16;
+  cudaStream_t s = fd::as_stream(stream);
+  const bf16 *xb = (const bf16*)x, *wb = (const bf16*)w;
+  bf16 *zb = (bf16*)z, *yb = (bf16*)y;
+  if (Cout % 128 == 0) return sg::launch_tma<128>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+  if (Cout % 64 == 0) return sg::launch_tma<64>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+  if (Cout % 32 == 0) return sg::launch_tma<32>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+  return sg::launch_tma<16>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
 }
 
 int sg_tc_status(unsigned* out, int clear) {

@@ -87,11 +87,13 @@ class UNet:
                  conv: str = "auto"):
         """``conv`` selects the forward and data-gradient convolution kernel:
         "tcgen05" (fifth-generation tensor cores, accumulator in tensor
-        memory), "mma" (warp-level tensor-core instructions) or "auto" (both
-        timed once per convolution shape at first use, the faster kept); the
-        weight gradient always uses the warp-level kernel."""
-        if conv not in ("tcgen05", "mma", "auto"):
-            raise ValueError("conv must be 'tcgen05', 'mma' or 'auto'")
+        memory), "tma" (the same fed by tensor-map boxes from one thread;
+        images whose width is a multiple of 128, the others fall back to
+        "tcgen05"), "mma" (warp-level tensor-core instructions) or "auto" (all
+        that take the shape timed once per convolution shape at first use, the
+        fastest kept); the weight gradient always uses the warp-level kernel."""
+        if conv not in ("tcgen05", "tma", "mma", "auto"):
+            raise ValueError("conv must be 'tcgen05', 'tma', 'mma' or 'auto'")
         self.conv = conv
         self.conv_choice = {}  # (N, H, W, Cin, Cout) -> kernel name, filled by "auto"
         self.widths = tuple(widths)
@@ -176,19 +178,28 @@ class UNet:
         self._buf[key] = B
         return B
 
-    _KERNELS = {"mma": "sg_conv3x3", "tcgen05": "sg_conv3x3_tc"}
+    _KERNELS = {"mma": "sg_conv3x3", "tcgen05": "sg_conv3x3_tc", "tma": "sg_conv3x3_tma"}
+
+    @staticmethod
+    def _takes(kernel, w, ci, co):
+        """Whether a kernel takes the shape (the TMA-fed one: widths that are
+        multiples of 128, channel counts that are multiples of 16)."""
+        return kernel != "tma" or (w % 128 == 0 and ci % 16 == 0 and co % 16 == 0)
 
     def _run_conv(self, x, N, h, w, ci, wt, bias, co, act, z, y):
         """One 3x3 convolution with the kernel chosen for its shape."""
         key = (N, h, w, ci, co)
         args = (_p(x), N, h, w, ci, _p(wt), _p(bias), co, act, _p(z), _p(y), _s())
         if self.conv != "auto":
-            fn = self._KERNELS[self.conv]
+            k = self.conv if self._takes(self.conv, w, ci, co) else "tcgen05"
+            fn = self._KERNELS[k]
         elif key in self.conv_choice:
             fn = self.conv_choice[key]
-        else:  # time both once on the real operands; the last call's result stands
+        else:  # time each kernel that takes the shape once on the real operands; the last call's result stands
             best = None
-            for fn in self._KERNELS.values():
+            for k, fn in self._KERNELS.items():
+                if not self._takes(k, w, ci, co):
+                    continue
                 L.call(fn, *args)
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record()

@@ -39,6 +39,14 @@ int sg_conv3x3_tc(const void* x, int N, int H, int W, int Cin, const void* w, co
                   void* z, void* y, void* stream);
 int sg_tc_status(unsigned* out, int clear);
 
+/* sg_conv3x3_tc fed by the tensor memory accelerator: one thread loads the
+ * operands as tensor-map boxes (zero fill outside the image = the padding) into
+ * a ring of stages and issues the MMAs as each lands.  Same arguments and
+ * results; needs W a multiple of 128 and Cin, Cout multiples of 16
+ * (FD_ERR_SHAPE otherwise).  Its waits share sg_tc_status's error word. */
+int sg_conv3x3_tma(const void* x, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout, int act,
+                   void* z, void* y, void* stream);
+
 /* wt[ci][ky][kx][co] = w[co][2-ky][2-kx][ci]: the weights of the data-gradient
  * convolution (dx = sg_conv3x3(dz, wt)). */
 int sg_flip_weights(const void* w, int Cin, int Cout, void* wt, void* stream);
