@@ -715,6 +715,9 @@ inline int encode_conv_maps(ConvMaps& m, const bf16* x, int N, int H, int W, int
 #ifndef SG_TMA_PAIR
 #define SG_TMA_PAIR 1
 #endif
+#ifndef SG_TMA_BN_MAX  // output channels of the widest tile (128 or 64)
+#define SG_TMA_BN_MAX 128
+#endif
 constexpr int kSmPerSmBytes = 233472;  // shared memory of an SM (228 KB), 1 KB of it reserved per CTA
 
 template <int BN, int R, int S>
@@ -874,7 +877,7 @@ int sg_conv3x3_tma(const void* x, int N, int H, int W, int Cin, const void* w, c
   cudaStream_t s = fd::as_stream(stream);
   const bf16 *xb = (const bf16*)x, *wb = (const bf16*)w;
   bf16 *zb = (bf16*)z, *yb = (bf16*)y;
-  if (Cout % 128 == 0) return sg::launch_tma<128>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+  if (SG_TMA_BN_MAX >= 128 && Cout % 128 == 0) return sg::launch_tma<128>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   if (Cout % 64 == 0) return sg::launch_tma<64>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   if (Cout % 32 == 0) return sg::launch_tma<32>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   return sg::launch_tma<16>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
