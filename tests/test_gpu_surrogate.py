@@ -82,17 +82,21 @@ def test_conv_gradients_match_oracle(cin, cout):
     assert np.abs(dx.float().cpu().numpy() - dxr).max() <= 1e-2 * np.abs(dxr).max()
 
 
-def test_network_gradients_match_oracle():
+@pytest.mark.parametrize("conv,W", [("auto", 32), ("tma", 128)])
+def test_network_gradients_match_oracle(conv, W):
+    """Loss and every layer's gradients against the oracle; with conv="tma"
+    the forward and data-gradient convolutions of the full-width level run on
+    the TMA-fed kernel (the narrower levels fall back to the tcgen05 one)."""
     from fingering_dynamics_gb300.surrogate import UNet
     widths = (16, 16, 32, 32)
-    net = UNet(widths, seed=3)
+    net = UNet(widths, seed=3, conv=conv)
     rng = np.random.default_rng(5)
     # a non-zero output layer so that every layer carries gradient
     net.w["out"] = torch.from_numpy(rng.normal(0, 0.05, net.w["out"].shape).astype(np.float32)).cuda()
     for n in net.b:
         net.b[n] = torch.from_numpy(rng.normal(0, 0.05, net.b[n].shape).astype(np.float32)).cuda()
     net.w16 = {n: t.to(torch.bfloat16) for n, t in net.w.items()}
-    N, H, W = 2, 16, 32
+    N, H = 2, 16
     x = rng.normal(size=(N, H, W, 16))
     x[..., 3] = (rng.random((N, H, W)) < 0.2)
     x[..., 4:] = 0
