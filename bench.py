@@ -715,7 +715,7 @@ def main():
     ap.add_argument("--frames", type=int, default=41, help="surrogate: frames per member (one per 200 iterations)")
     ap.add_argument("--train-steps", type=int, default=1000, help="surrogate: timed AdamW steps")
     ap.add_argument("--batch", type=int, default=32, help="surrogate: training batch")
-    ap.add_argument("--conv", default="auto", choices=["auto", "mma", "tcgen05"],
+    ap.add_argument("--conv", default="auto", choices=["auto", "mma", "tcgen05", "tma"],
                     help="surrogate: forward / data-gradient convolution kernel (auto: the faster per shape)")
     ap.add_argument("--save-net", default=None, help="surrogate: write the trained network's weights (.npz) here")
     ap.add_argument("--load-net", default=None,
