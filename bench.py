@@ -667,8 +667,9 @@ def run_convs(args):
         z = torch.empty_like(y)
         fl = 2.0 * 9 * ci * co * N * H * W
         line = {"metric": "conv3x3 throughput", "unit": "TFLOP/s", "shape": [N, H, W, ci, co]}
-        for fn, key in (("sg_conv3x3", "mma"), ("sg_conv3x3_tc", "tcgen05"), ("sg_conv3x3_tma", "tma")):
-            if key == "tma" and W % 128:
+        for fn, key in (("sg_conv3x3", "mma"), ("sg_conv3x3_tc", "tcgen05"), ("sg_conv3x3_tma", "tma"),
+                        ("sg_conv3x3_tma_ws", "tma_ws")):
+            if key.startswith("tma") and W % 128:
                 continue
             for _ in range(args.warmup):
                 L.call(fn, p(x), N, H, W, ci, p(w), None, co, 1, p(z), p(y), None)
@@ -715,7 +716,7 @@ def main():
     ap.add_argument("--frames", type=int, default=41, help="surrogate: frames per member (one per 200 iterations)")
     ap.add_argument("--train-steps", type=int, default=1000, help="surrogate: timed AdamW steps")
     ap.add_argument("--batch", type=int, default=32, help="surrogate: training batch")
-    ap.add_argument("--conv", default="auto", choices=["auto", "mma", "tcgen05", "tma"],
+    ap.add_argument("--conv", default="auto", choices=["auto", "mma", "tcgen05", "tma", "tma_ws"],
                     help="surrogate: forward / data-gradient convolution kernel (auto: the faster per shape)")
     ap.add_argument("--save-net", default=None, help="surrogate: write the trained network's weights (.npz) here")
     ap.add_argument("--load-net", default=None,

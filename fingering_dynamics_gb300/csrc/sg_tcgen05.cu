@@ -32,6 +32,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "../../include/fdsurrogate.h"
 #include "fd_host.h"
 #include "fd_tmap.h"
@@ -527,8 +529,8 @@ struct ConvMaps {
   CUtensorMap x, w;
 };
 
-template <int BN, int R, int S>
-struct TmaConvCfg {
+template <int BN, int R>
+struct TmaStage {
   static constexpr int A_BOX = (R + 2) * kHaloPx * 16;      // bytes of one A box
   static constexpr int SLICE = (A_BOX + 127) / 128 * 128;   // one 8-channel slice of the halo
   static constexpr int ROWB = kHaloPx * 16;                 // one input row of a slice
@@ -537,12 +539,17 @@ struct TmaConvCfg {
   static constexpr int TB = 2 * BSL;                        // one tap's weights
   static constexpr int STAGE = A_BYTES + 9 * TB;
   static constexpr int TX = 2 * A_BOX + 18 * BSL;           // bytes the boxes of a stage bring
-  static constexpr int OFF_BAR = S * STAGE;
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "tile");
+  static_assert(STAGE % 128 == 0 && SLICE % 128 == 0 && BSL % 128 == 0, "128-byte aligned box destinations");
+};
+
+template <int BN, int R, int S>
+struct TmaConvCfg : TmaStage<BN, R> {
+  static constexpr int OFF_BAR = S * TmaStage<BN, R>::STAGE;
   static constexpr int SMEM = OFF_BAR + 2 * S * 8 + 16 + 128;  // + mbarriers, TMEM address, alignment
   static constexpr int NCOL = R * BN;
   static constexpr int COLS = NCOL <= 32 ? 32 : (NCOL <= 64 ? 64 : (NCOL <= 128 ? 128 : (NCOL <= 256 ? 256 : 512)));
-  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256 && NCOL <= 512, "tile");
-  static_assert(STAGE % 128 == 0 && SLICE % 128 == 0 && BSL % 128 == 0, "128-byte aligned box destinations");
+  static_assert(NCOL <= 512, "tile");
 };
 
 // shared memory of TmaConvCfg<BN, R, S> (the stage count that fits is chosen
@@ -787,6 +794,252 @@ int launch_tma(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const
   return launch_tma_s<BN, 1>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent, warp-specialised variant (sg_conv3x3_tma_ws).  The CTA keeps
+// two accumulator buffers of R x BN TMEM columns and walks its tiles (tile =
+// CTA index + k x grid; the output-channel tiles of a pixel tile are
+// consecutive, so CTAs that run at the same time share the input halo through
+// L2).  Warp 8 (one thread) issues the boxes and MMAs of the CTA's chunk
+// sequence (tile j, chunk kc) -> c = j x nk + kc through the same ring of S
+// stages, the ring running on across tile boundaries; after a tile's last
+// MMAs it commits the tile's accumulator buffer to accf[j % 2].  Warps 0..7
+// (warp w: TMEM lanes 32 (w % 4) .. + 31 = pixels of each row, the 16-column
+// groups w / 4, w / 4 + 2, ...) wait for accf, read the accumulators, add the
+// bias, apply GELU, store, and arrive on acce[j % 2] (one arrival per warp);
+// the MMAs of tile j + 2 wait for it.  So one tile's epilogue overlaps the
+// next tile's MMAs and the next tiles' loads.
+// ---------------------------------------------------------------------------
+constexpr int kWsEpiWarps = 8;
+constexpr int kWsThreads = 32 * (kWsEpiWarps + 1);
+
+template <int BN, int R, int S>
+struct WsCfg : TmaStage<BN, R> {
+  static constexpr int OFF_BAR = S * TmaStage<BN, R>::STAGE;
+  static constexpr int SMEM = OFF_BAR + (2 * S + 4) * 8 + 16 + 128;
+  static constexpr int NCOL = 2 * R * BN;  // two accumulator buffers
+  static constexpr int COLS = NCOL <= 32 ? 32 : (NCOL <= 64 ? 64 : (NCOL <= 128 ? 128 : (NCOL <= 256 ? 256 : 512)));
+  static_assert(NCOL <= 512, "two accumulator buffers in tensor memory");
+};
+
+constexpr int ws_conv_smem(int BN, int R, int S) {
+  return S * (2 * (((R + 2) * kHaloPx * 16 + 127) / 128 * 128) + 18 * BN * 16) + (2 * S + 4) * 8 + 16 + 128;
+}
+
+template <int BN, int R, int S>
+__global__ void __launch_bounds__(kWsThreads, 1) k_conv3x3_tma_ws(const __grid_constant__ ConvMaps maps, int N, int H,
+                                                                 int W, int Cin, const float* __restrict__ bias,
+                                                                 int Cout, int act, bf16* __restrict__ z,
+                                                                 bf16* __restrict__ y) {
+  using C = TmaStage<BN, R>;
+  using WC = WsCfg<BN, R, S>;
+  extern __shared__ char smem_raw[];
+  char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + WC::OFF_BAR);
+  uint64_t* empty = full + S;
+  uint64_t* accf = empty + S;  // [2]
+  uint64_t* acce = accf + 2;   // [2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tiles_x = W / kTcBM;
+  const int nco = Cout / BN;
+  const int ntiles = N * (H / R) * tiles_x * nco;
+  const int nk = Cin / 16;
+  const int mine = blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;  // tiles of this CTA
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(WC::COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 2 * S + 2; ++i) mbar_init(&full[i]);  // full, empty, accf: one arrival each
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acce[0])), "n"(kWsEpiWarps) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acce[1])), "n"(kWsEpiWarps) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  // tile j of this CTA -> (first output row n*H + yy, x0, co0)
+  auto tile_of = [&](int j, int& row, int& x0, int& co0) {
+    const int t = (int)blockIdx.x + j * (int)gridDim.x;
+    const int pt = t / nco;
+    co0 = (t % nco) * BN;
+    x0 = (pt % tiles_x) * kTcBM;
+    row = (pt / tiles_x) * R;
+  };
+
+  if (warp == kWsEpiWarps) {
+    if (lane == 0) {
+      const int nc = mine * nk;  // chunks of this CTA
+      int pend_full[S], pend_empty[S];
+#pragma unroll
+      for (int i = 0; i < S; ++i) pend_full[i] = pend_empty[i] = -1;
+      auto issue = [&](int c, int st) {
+        int row, x0, co0;
+        tile_of(c / nk, row, x0, co0);
+        const int kc = c % nk, n = row / H, yy = row % H;
+        char* As = smem + st * C::STAGE;
+        char* Bs = As + C::A_BYTES;
+        mbar_expect_tx(&full[st], (unsigned)C::TX);
+#pragma unroll
+        for (int s = 0; s < 2; ++s) tma_load_4d(As + s * C::SLICE, &maps.x, kc * 16 + 8 * s, x0 - 1, yy - 1, n, &full[st]);
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap)
+#pragma unroll
+          for (int s = 0; s < 2; ++s)
+            tma_load_3d(Bs + tap * C::TB + s * C::BSL, &maps.w, kc * 16 + 8 * s, tap, co0, &full[st]);
+        pend_full[st] = c;
+      };
+      constexpr uint32_t idesc = instr_desc<kTcBM, BN>();
+      bool ok = true;
+      for (int c = 0; c < S && c < nc; ++c) issue(c, c);
+      for (int c = 0; c < nc && ok; ++c) {
+        const int j = c / nk, kc = c % nk, b = j & 1, st = c % S;
+        if (kc == 0 && j >= 2) {  // buffer b: the epilogue of tile j - 2 has read it
+          ok = mbar_wait_ok(&acce[b], (unsigned)((j - 2) >> 1) & 1u, true);
+          if (!ok) break;
+        }
+        ok = mbar_wait_ok(&full[st], (unsigned)(c / S) & 1u, true);
+        if (!ok) break;
+        pend_full[st] = -1;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a0 = smem_u32(smem + st * C::STAGE), b0 = a0 + C::A_BYTES;
+        const uint32_t d0 = tmem + (uint32_t)(b * R * BN);
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+          const int ky = tap / 3, kx = tap % 3;
+          const uint64_t bd = smem_desc(b0 + tap * C::TB, C::BSL, 128);
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const uint64_t ad = smem_desc(a0 + (r + ky) * C::ROWB + kx * 16, C::SLICE, 128);
+            tc_mma(d0 + (uint32_t)(r * BN), ad, bd, idesc, (kc > 0 || tap > 0) ? 1u : 0u);
+          }
+        }
+        tc_commit(&empty[st]);
+        pend_empty[st] = c;
+        if (kc == nk - 1) tc_commit(&accf[b]);  // tile j's accumulators are complete
+        if (c >= 1 && c - 1 + S < nc) {        // refill the stage of chunk c-1
+          const int ps = (c - 1) % S;
+          ok = mbar_wait_ok(&empty[ps], (unsigned)((c - 1) / S) & 1u, true);
+          if (!ok) break;
+          pend_empty[ps] = -1;
+          issue(c - 1 + S, ps);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        if (pend_full[i] >= 0) mbar_wait_ok(&full[i], (unsigned)(pend_full[i] / S) & 1u, false);
+        if (pend_empty[i] >= 0) mbar_wait_ok(&empty[i], (unsigned)(pend_empty[i] / S) & 1u, false);
+      }
+    }
+    __syncwarp();
+  } else {
+    // epilogue: warp w reads TMEM lanes 32 q .. 32 q + 31 (pixels x0 + 32 q + lane of each row, q = w % 4),
+    // 16-column groups h, h + 2, ... (h = w / 4)
+    const int q = warp & 3, h = warp >> 2;
+    for (int j = 0; j < mine; ++j) {
+      const int b = j & 1;
+      int row, x0, co0;
+      tile_of(j, row, x0, co0);
+      mbar_wait_ok(&accf[b], (unsigned)(j >> 1) & 1u, true);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+      for (int r = 0; r < R; ++r) {
+        const long long p = ((long long)(row + r) * W + x0) + q * 32 + lane;
+#pragma unroll
+        for (int c0 = 16 * h; c0 < BN; c0 += 32) {
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * R * BN + r * BN + c0), v);
+          const int co = co0 + c0;
+          uint32_t zw[8], yw[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            float t0 = v[2 * i] + (bias ? bias[co + 2 * i] : 0.0f);
+            float t1 = v[2 * i + 1] + (bias ? bias[co + 2 * i + 1] : 0.0f);
+            const __nv_bfloat162 zp = __floats2bfloat162_rn(t0, t1);
+            zw[i] = *reinterpret_cast<const uint32_t*>(&zp);
+            if (act == SG_ACT_GELU) {
+              t0 = gelu_f(t0);
+              t1 = gelu_f(t1);
+            }
+            const __nv_bfloat162 yp = __floats2bfloat162_rn(t0, t1);
+            yw[i] = *reinterpret_cast<const uint32_t*>(&yp);
+          }
+          const size_t o = (size_t)p * Cout + co;
+          if (z) {
+            reinterpret_cast<uint4*>(z + o)[0] = make_uint4(zw[0], zw[1], zw[2], zw[3]);
+            reinterpret_cast<uint4*>(z + o)[1] = make_uint4(zw[4], zw[5], zw[6], zw[7]);
+          }
+          if (y) {
+            reinterpret_cast<uint4*>(y + o)[0] = make_uint4(yw[0], yw[1], yw[2], yw[3]);
+            reinterpret_cast<uint4*>(y + o)[1] = make_uint4(yw[4], yw[5], yw[6], yw[7]);
+          }
+        }
+      }
+      // this warp's reads of buffer b are complete (tcgen05.wait::ld in tmem_ld16)
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acce[b])) : "memory");
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(WC::COLS) : "memory");
+  }
+}
+
+template <int BN, int R, int S>
+int launch_ws_r(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
+                bf16* z, bf16* y, cudaStream_t s) {
+  using WC = WsCfg<BN, R, S>;
+  static_assert(WC::SMEM <= 227 * 1024 && WC::SMEM == ws_conv_smem(BN, R, S), "shared memory");
+  auto kern = k_conv3x3_tma_ws<BN, R, S>;
+  static std::atomic<unsigned long long> attr_done{0};
+  if (fd::ensure_smem_attr(kern, 227 * 1024, attr_done) != cudaSuccess)
+    return fd::check_launch("sg_conv3x3_tma_ws: shared-memory attribute");
+  int smem = WC::SMEM;
+  const int fit = 512 / WC::COLS;  // CTAs per SM whose accumulators fit the tensor memory
+  if (kSmPerSmBytes / (smem + 1024) > fit) smem = kSmPerSmBytes / (fit + 1) - 1024 + 1;
+  if (smem > 227 * 1024) smem = 227 * 1024;
+  int per_sm = 1, dev = 0, sms = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWsThreads, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long ntiles = (long long)N * (H / R) * (W / kTcBM) * (Cout / BN);
+  const long long grid = std::min<long long>(ntiles, (long long)sms * per_sm);
+  ConvMaps maps;
+  if (int r = encode_conv_maps(maps, x, N, H, W, Cin, w, Cout, R, BN)) return r;
+  kern<<<(unsigned)grid, kWsThreads, smem, s>>>(maps, N, H, W, Cin, b, Cout, act, z, y);
+  return fd::check_launch("sg_conv3x3_tma_ws");
+}
+
+// the most stages (up to six) that fit one CTA
+template <int BN, int R>
+int launch_ws_s(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
+                bf16* z, bf16* y, cudaStream_t s) {
+  if constexpr (ws_conv_smem(BN, R, 6) <= 227 * 1024) return launch_ws_r<BN, R, 6>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  else if constexpr (ws_conv_smem(BN, R, 5) <= 227 * 1024) return launch_ws_r<BN, R, 5>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  else return launch_ws_r<BN, R, 4>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+}
+
+// rows per tile: the most of 4, 2, 1 that divide H with two buffers of R x BN
+// accumulator columns in the tensor memory
+template <int BN>
+int launch_ws(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
+              bf16* z, bf16* y, cudaStream_t s) {
+  if constexpr (2 * 4 * BN <= 512) {
+    if (H % 4 == 0) return launch_ws_s<BN, 4>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  }
+  if (H % 2 == 0) return launch_ws_s<BN, 2>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+  return launch_ws_s<BN, 1>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
+}
+
 template <int BN, int BK, int R>
 int launch_tch_r(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
                  bf16* z, bf16* y, cudaStream_t s) {
@@ -881,6 +1134,25 @@ int sg_conv3x3_tma(const void* x, int N, int H, int W, int Cin, const void* w, c
   if (Cout % 64 == 0) return sg::launch_tma<64>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   if (Cout % 32 == 0) return sg::launch_tma<32>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   return sg::launch_tma<16>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+}
+
+int sg_conv3x3_tma_ws(const void* x, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout,
+                      int act, void* z, void* y, void* stream) {
+  FD_REQUIRE(x && w && (z || y) && N > 0 && H > 0 && W > 0, FD_ERR_ARG, "sg_conv3x3_tma_ws: bad arguments");
+  FD_REQUIRE(W % sg::kTcBM == 0 && Cin % 16 == 0 && Cout % 16 == 0 && Cin > 0 && Cout > 0, FD_ERR_SHAPE,
+             "sg_conv3x3_tma_ws: needs W a multiple of 128 and channel counts multiples of 16 (got W=%d, %d -> %d)",
+             W, Cin, Cout);
+  FD_REQUIRE(act == SG_ACT_NONE || act == SG_ACT_GELU, FD_ERR_ARG, "sg_conv3x3_tma_ws: activation %d", act);
+  FD_REQUIRE(((uintptr_t)x | (uintptr_t)w | (uintptr_t)z | (uintptr_t)y) % 16 == 0, FD_ERR_ARG,
+             "sg_conv3x3_tma_ws: tensors must be 16-byte aligned");
+  using sg::bf16;
+  cudaStream_t s = fd::as_stream(stream);
+  const bf16 *xb = (const bf16*)x, *wb = (const bf16*)w;
+  bf16 *zb = (bf16*)z, *yb = (bf16*)y;
+  if (Cout % 128 == 0) return sg::launch_ws<128>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+  if (Cout % 64 == 0) return sg::launch_ws<64>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+  if (Cout % 32 == 0) return sg::launch_ws<32>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+  return sg::launch_ws<16>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
 }
 
 int sg_tc_status(unsigned* out, int clear) {

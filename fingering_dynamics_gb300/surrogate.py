@@ -89,11 +89,12 @@ class UNet:
         "tcgen05" (fifth-generation tensor cores, accumulator in tensor
         memory), "tma" (the same fed by tensor-map boxes from one thread;
         images whose width is a multiple of 128, the others fall back to
-        "tcgen05"), "mma" (warp-level tensor-core instructions) or "auto" (all
+        "tcgen05"), "tma_ws" (its persistent warp-specialised form, same
+        shapes), "mma" (warp-level tensor-core instructions) or "auto" (all
         that take the shape timed once per convolution shape at first use, the
         fastest kept); the weight gradient always uses the warp-level kernel."""
-        if conv not in ("tcgen05", "tma", "mma", "auto"):
-            raise ValueError("conv must be 'tcgen05', 'tma', 'mma' or 'auto'")
+        if conv not in ("tcgen05", "tma", "tma_ws", "mma", "auto"):
+            raise ValueError("conv must be 'tcgen05', 'tma', 'tma_ws', 'mma' or 'auto'")
         self.conv = conv
         self.conv_choice = {}  # (N, H, W, Cin, Cout) -> kernel name, filled by "auto"
         self.widths = tuple(widths)
@@ -178,13 +179,14 @@ class UNet:
         self._buf[key] = B
         return B
 
-    _KERNELS = {"mma": "sg_conv3x3", "tcgen05": "sg_conv3x3_tc", "tma": "sg_conv3x3_tma"}
+    _KERNELS = {"mma": "sg_conv3x3", "tcgen05": "sg_conv3x3_tc", "tma": "sg_conv3x3_tma",
+                "tma_ws": "sg_conv3x3_tma_ws"}
 
     @staticmethod
     def _takes(kernel, w, ci, co):
-        """Whether a kernel takes the shape (the TMA-fed one: widths that are
+        """Whether a kernel takes the shape (the TMA-fed ones: widths that are
         multiples of 128, channel counts that are multiples of 16)."""
-        return kernel != "tma" or (w % 128 == 0 and ci % 16 == 0 and co % 16 == 0)
+        return not kernel.startswith("tma") or (w % 128 == 0 and ci % 16 == 0 and co % 16 == 0)
 
     def _run_conv(self, x, N, h, w, ci, wt, bias, co, act, z, y):
         """One 3x3 convolution with the kernel chosen for its shape."""

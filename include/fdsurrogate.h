@@ -47,6 +47,13 @@ int sg_tc_status(unsigned* out, int clear);
 int sg_conv3x3_tma(const void* x, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout, int act,
                    void* z, void* y, void* stream);
 
+/* sg_conv3x3_tma as a persistent kernel with warp-specialised roles: one
+ * thread issues the boxes and MMAs of the CTA's tiles through one ring, two
+ * accumulator buffers in tensor memory let four epilogue warps finish a tile
+ * while the next one is multiplied.  Same arguments, results and shape rule. */
+int sg_conv3x3_tma_ws(const void* x, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout,
+                      int act, void* z, void* y, void* stream);
+
 /* wt[ci][ky][kx][co] = w[co][2-ky][2-kx][ci]: the weights of the data-gradient
  * convolution (dx = sg_conv3x3(dz, wt)). */
 int sg_flip_weights(const void* w, int Cin, int Cout, void* wt, void* stream);

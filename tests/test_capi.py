@@ -106,9 +106,10 @@ def test_new_entry_points_check_their_arguments_on_the_host(lib):
     vp = ctypes.c_void_p
     for w, cin, cout, code in ((64, 16, 16, -2), (128, 24, 16, -2), (128, 16, 40, -2), (128, 16, 16, -1)):
         act = 5 if code == -1 else 1  # unknown activation
-        with pytest.raises(L.FDError) as e:
-            L.call("sg_conv3x3_tma", vp(256), 1, 4, w, cin, vp(512), None, cout, act, None, vp(768), None)
-        assert e.value.code == code
+        for fn in ("sg_conv3x3_tma", "sg_conv3x3_tma_ws"):
+            with pytest.raises(L.FDError) as e:
+                L.call(fn, vp(256), 1, 4, w, cin, vp(512), None, cout, act, None, vp(768), None)
+            assert e.value.code == code
 
 
 def test_integration_stub_struct_matches_the_binding():

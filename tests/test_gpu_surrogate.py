@@ -82,7 +82,7 @@ def test_conv_gradients_match_oracle(cin, cout):
     assert np.abs(dx.float().cpu().numpy() - dxr).max() <= 1e-2 * np.abs(dxr).max()
 
 
-@pytest.mark.parametrize("conv,W", [("auto", 32), ("tma", 128)])
+@pytest.mark.parametrize("conv,W", [("auto", 32), ("tma", 128), ("tma_ws", 128)])
 def test_network_gradients_match_oracle(conv, W):
     """Loss and every layer's gradients against the oracle; with conv="tma"
     the forward and data-gradient convolutions of the full-width level run on
@@ -218,7 +218,8 @@ def test_tcgen05_conv_matches_oracle(n, h, w, cin, cout, act):
                                                 (1, 3, 128, 96, 32, 1), (1, 2, 128, 16, 16, 0),
                                                 (2, 4, 128, 128, 128, 1), (1, 8, 256, 384, 128, 0),
                                                 (1, 4, 256, 32, 96, 1)])
-def test_tma_conv_matches_oracle(n, h, w, cin, cout, act):
+@pytest.mark.parametrize("kernel", ["sg_conv3x3_tma", "sg_conv3x3_tma_ws"])
+def test_tma_conv_matches_oracle(kernel, n, h, w, cin, cout, act):
     """The TMA-fed tcgen05 convolution (tensor-map boxes into a ring of
     stages, zero fill as the padding) against the oracle and against the
     halo-tile tcgen05 kernel; covers 1, 2 and 4 rows per tile, 2, 3 and 4
@@ -229,7 +230,7 @@ def test_tma_conv_matches_oracle(n, h, w, cin, cout, act):
     b = rng.normal(0, 0.1, cout).astype(np.float32)
     bd = torch.from_numpy(b).cuda()
     outs = {}
-    for name in ("sg_conv3x3_tma", "sg_conv3x3_tc"):
+    for name in (kernel, "sg_conv3x3_tc"):
         z = torch.zeros((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
         y = torch.zeros_like(z)
         _call(name, _p(x), n, h, w, cin, _p(wt), _p(bd), cout, act, _p(z), _p(y), None)
@@ -239,7 +240,7 @@ def test_tma_conv_matches_oracle(n, h, w, cin, cout, act):
     zr = U.conv3x3(xh, wh, b.astype(np.float64))
     yr = U.gelu(zr) if act else zr
     scale = np.abs(zr).max()
-    zt, yt = outs["sg_conv3x3_tma"]
+    zt, yt = outs[kernel]
     assert np.abs(zt - zr).max() <= 1e-2 * scale
     assert np.abs(yt - yr).max() <= 1e-2 * scale
     # the same products summed in another order: the bfloat16 results agree almost everywhere
