@@ -809,6 +809,9 @@ int launch_tma(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const
 // the MMAs of tile j + 2 wait for it.  So one tile's epilogue overlaps the
 // next tile's MMAs and the next tiles' loads.
 // ---------------------------------------------------------------------------
+#ifndef SG_WS_BN_MAX  // output channels of the persistent kernel's widest tile (128 or 64)
+#define SG_WS_BN_MAX 128
+#endif
 constexpr int kWsEpiWarps = 8;
 constexpr int kWsThreads = 32 * (kWsEpiWarps + 1);
 
@@ -1149,7 +1152,7 @@ int sg_conv3x3_tma_ws(const void* x, int N, int H, int W, int Cin, const void* w
   cudaStream_t s = fd::as_stream(stream);
   const bf16 *xb = (const bf16*)x, *wb = (const bf16*)w;
   bf16 *zb = (bf16*)z, *yb = (bf16*)y;
-  if (Cout % 128 == 0) return sg::launch_ws<128>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+  if (SG_WS_BN_MAX >= 128 && Cout % 128 == 0) return sg::launch_ws<128>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   if (Cout % 64 == 0) return sg::launch_ws<64>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   if (Cout % 32 == 0) return sg::launch_ws<32>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   return sg::launch_ws<16>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
