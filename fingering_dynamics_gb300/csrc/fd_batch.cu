@@ -70,12 +70,19 @@ int prepare(fd_batch* b) {
     return check_launch("fd_batch: shared-memory attribute");
   std::vector<BatchInst<SF>> hi(b->n);
   std::vector<int4> tiles;
+  // members already flagged non-finite are not stepped any more: leave their
+  // tiles out, so that the live members' tiles share the persistent grid
+  std::vector<unsigned> flagged((size_t)b->n, 0u);
+  if (cudaDeviceSynchronize() != cudaSuccess ||
+      cudaMemcpy(flagged.data(), b->d_status, (size_t)b->n * sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return check_launch("fd_batch: member status");
   for (int i = 0; i < b->n; ++i) {
     hi[i].args[0] = instance_args<SF>(b->inst[i], b->st, b->rows, false, b->d_status + i);
     hi[i].args[1] = instance_args<SF>(b->inst[i], b->st, b->rows, true, b->d_status + i);
     if (int r = tma_maps<SF, NT>(hi[i].args[0], (const char*)b->inst[i].pop_a, hi[i].maps[0])) return r;
     if (int r = tma_maps<SF, NT>(hi[i].args[1], (const char*)b->inst[i].pop_b, hi[i].maps[1])) return r;
     const int nb = (b->inst[i].prm.W + NT - 1) / NT, ns = hi[i].args[0].nstrips;
+    if (flagged[(size_t)i] != 0u) continue;
     for (int s = 0; s < ns; ++s)
       for (int bb = 0; bb < nb; ++bb) tiles.push_back(make_int4(i, bb, s, 0));
   }
@@ -93,10 +100,11 @@ int prepare(fd_batch* b) {
   b->d_inst = nullptr;
   b->d_tiles = nullptr;
   if (cudaMalloc(&b->d_inst, sizeof(BatchInst<SF>) * hi.size()) != cudaSuccess ||
-      cudaMalloc(&b->d_tiles, sizeof(int4) * tiles.size()) != cudaSuccess)
+      cudaMalloc(&b->d_tiles, sizeof(int4) * (tiles.empty() ? 1 : tiles.size())) != cudaSuccess)
     return check_launch("fd_batch: table allocation");
   if (cudaMemcpy(b->d_inst, hi.data(), sizeof(BatchInst<SF>) * hi.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(b->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+      (!tiles.empty() &&
+       cudaMemcpy(b->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice) != cudaSuccess))
     return check_launch("fd_batch: table upload");
   b->ntiles = (int)tiles.size();
   int per_sm = 1, dev = 0, sms = 1;

@@ -213,9 +213,14 @@ class Ensemble:
             lat.iteration += n
         return e0.elapsed_time(e1) / 1e3
 
+    def _live_sizes(self) -> list:
+        """(H, W) of the members the batch still steps (not flagged non-finite)."""
+        return [(lat.H, lat.W) for lat, q in zip(self.lattices, self.member_status()) if not q]
+
     def tiles_for(self, band_width: int, rows_per_strip: int) -> int:
-        """Tiles per iteration of the shape (as fd_batch builds them)."""
-        return tile_count([(lat.H, lat.W) for lat in self.lattices], band_width, rows_per_strip)
+        """Tiles per iteration of the shape (as fd_batch builds them: members
+        flagged non-finite are left out)."""
+        return tile_count(self._live_sizes(), band_width, rows_per_strip)
 
     def wave_candidates(self, bands=(64, 128, 256), max_rounds: int = 8, min_fill: float = 0.9) -> list:
         """Shapes whose tile count just fits a whole number of rounds of the
@@ -225,7 +230,7 @@ class Ensemble:
         just over a whole number of rounds leaves a last round in which a few
         CTAs run while the others wait (up to a fifth of the launch)."""
         keep = self.config
-        sizes = [(lat.H, lat.W) for lat in self.lattices]
+        sizes = self._live_sizes()
         out = []
         for band in bands:
             self.configure(band, 64)

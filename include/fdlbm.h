@@ -340,7 +340,10 @@ typedef struct fd_batch fd_batch;
 int fd_batch_create(const fd_instance* inst, int n, const fd_storage* st, int rows_per_strip, int band_width,
                     fd_batch** out);
 
-/* Change the tile shape (drops a captured graph). */
+/* Change the tile shape (drops a captured graph).  The new tile table leaves
+ * out the members flagged non-finite (fd_batch_member_status), which the
+ * batch no longer steps, so that the live members' tiles share the persistent
+ * grid; a member whose flag was cleared is taken back by the next call. */
 int fd_batch_configure(fd_batch* b, int rows_per_strip, int band_width);
 
 /* Advance every member nsteps iterations on `stream`.  use_graph != 0 replays

@@ -74,7 +74,8 @@ def test_quarantine_of_a_non_finite_member():
     """One member of a batch made non-finite on the host: the batch flags that
     member only (fd_batch_member_status), skips it from then on (its buffers
     no longer change), and every other member stays bit-identical to the same
-    lattice stepped alone."""
+    lattice stepped alone, also after a new tile table has left the flagged
+    member out; clearing the flag and configuring again takes it back."""
     from fingering_dynamics_gb300.ensemble import Ensemble
     from fingering_dynamics_gb300.lattice import Lattice
     members = _members()[:4]
@@ -98,9 +99,31 @@ def test_quarantine_of_a_non_finite_member():
         got, ref = ens.lattices[k], solo[k]
         assert torch.equal(packed_planes(got.ppop[got.pcur], got.H, got.W, "f32"),
                            packed_planes(ref.ppop[ref.pcur], ref.H, ref.W, "f32")), k
+    # a new tile table leaves the quarantined member out; the others go on as before
+    full = ens.tiles
+    ens.configure(*ens.config)
+    assert ens.tiles == full - _member_tiles(bad, ens.config)
+    assert ens.tiles == ens.tiles_for(*ens.config)
+    ens.step(5)
+    torch.cuda.synchronize()
+    assert all(torch.equal(a, b) for a, b in zip(frozen, bad.ppop)), "a quarantined member was stepped"
+    for k in (0, 1, 3):
+        solo[k].advance(5)
+        torch.cuda.synchronize()
+        got, ref = ens.lattices[k], solo[k]
+        assert torch.equal(packed_planes(got.ppop[got.pcur], got.H, got.W, "f32"),
+                           packed_planes(ref.ppop[ref.pcur], ref.H, ref.W, "f32")), k
+    # clearing the flag and configuring again takes the member back
     assert ens.member_status(clear=True)[2]
     assert ens.member_status() == [False] * 4
+    ens.configure(*ens.config)
+    assert ens.tiles == full
     ens.close()
+
+
+def _member_tiles(lat, config):
+    from fingering_dynamics_gb300.ensemble import tile_count
+    return tile_count([(lat.H, lat.W)], *config)
 
 
 @pytest.mark.parametrize("W", [128, 92], ids=["staged_kernel", "register_kernel"])
