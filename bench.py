@@ -681,6 +681,24 @@ def run_convs(args):
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / args.steps
             line[key] = {"us": round(ms * 1e3, 1), "tflops": round(fl / ms / 1e9, 1)}
+        # the weight gradient of the same shape (dz = y here: same layout as the real gradient)
+        nparts = max(int(L.lib().sg_wgrad_partial_floats(N, H, W, ci, co)), 8 * co * 9 * ci)
+        part = torch.empty(nparts, dtype=torch.float32, device="cuda")
+        dw = torch.empty(co * 9 * ci, dtype=torch.float32, device="cuda")
+        for fn, key in (("sg_conv3x3_wgrad", "wgrad_mma"), ("sg_conv3x3_wgrad_tc", "wgrad_tcgen05")):
+            if key == "wgrad_tcgen05" and W % 128:
+                continue
+            wa = (p(x), p(y), N, H, W, ci, co, p(dw), p(part), part.numel(), 0, None)
+            for _ in range(args.warmup):
+                L.call(fn, *wa)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                L.call(fn, *wa)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            line[key] = {"us": round(ms * 1e3, 1), "tflops": round(fl / ms / 1e9, 1)}
         print(json.dumps(line), flush=True)
     return 0
 

@@ -115,6 +115,7 @@ SIGNATURES = {
     "sg_conv3x3_tma": [_VP, _I, _I, _I, _I, _VP, _VP, _I, _I, _VP, _VP, _VP],
     "sg_conv3x3_tma_ws": [_VP, _I, _I, _I, _I, _VP, _VP, _I, _I, _VP, _VP, _VP],
     "sg_conv3x3_wgrad": [_VP, _VP, _I, _I, _I, _I, _I, _VP, _VP, _SZ, _I, _VP],
+    "sg_conv3x3_wgrad_tc": [_VP, _VP, _I, _I, _I, _I, _I, _VP, _VP, _SZ, _I, _VP],
     "sg_wgrad_partial_floats": [_I, _I, _I, _I, _I],
     "sg_bias_grad": [_VP, _SZ, _I, _VP, _VP, _VP],
     "sg_bias_partial_floats": [_I],

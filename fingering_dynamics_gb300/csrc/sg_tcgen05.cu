@@ -1043,6 +1043,257 @@ int launch_ws(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const 
   return launch_ws_s<BN, 1>(x, N, H, W, Cin, w, b, Cout, act, z, y, s);
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient on tcgen05 (sg_conv3x3_wgrad_tc):
+//   dw[co][tap][ci] = sum_p dz[p][co] x[p + (ky-1, kx-1)][ci]
+// as D[co][ci] (M = 128 output channels, N = BN input channels, K = pixels)
+// per tap.  A CTA takes one kernel row ky (its three taps kx = 0..2, three
+// accumulators of BN TMEM columns), one output-channel tile, one input-channel
+// tile and a contiguous range of pixel chunks (128 pixels of one image row).
+// Both operands are channel-contiguous in memory, so they are MN-major (in
+// the matrix descriptor of an MN-major operand without swizzle, as of a
+// K-major one, LBO is the stride between core matrices along K and SBO the
+// stride between 8-row groups along M or N; the other reading of the two
+// fields fails the GPU tests):
+//   A: a dz box (8 channels x 128 pixels) per 8-channel group below Cout ->
+//      [pixel][8 channels], core matrices of 8 pixels 128 B apart along K
+//      (LBO), groups 2048 B apart (SBO); the groups at or beyond Cout are
+//      zeroed once and never loaded;
+//   B: an x box (8 channels x 130 pixels of row y + ky - 1) per 8-channel
+//      group, groups kWgBGrp apart (SBO); tap kx is the window 16 B x kx
+//      into it.
+// One thread issues the boxes of a ring of S stages and the 3 x 8 MMAs of a
+// chunk; the FP32 partial sums go to partial[split][co][tap][ci] and are
+// added in a fixed order afterwards, so the result does not depend on
+// scheduling.
+// ---------------------------------------------------------------------------
+constexpr int kWgBGrp = ((kHaloPx * 16 + 127) / 128) * 128;  // 2176 B: one 8-channel group of the x halo
+
+template <int BN, bool SW>
+struct WgTcCfg {
+  // SW: the input channels on M (x halo as A, dz as B), else the output channels
+  static constexpr int AGRP = SW ? kWgBGrp : 2048;          // bytes of one 8-channel group of A
+  static constexpr int BGRP = SW ? 2048 : kWgBGrp;          // and of B
+  static constexpr int A_BYTES = 16 * AGRP;                 // 128 channels
+  static constexpr int B_BYTES = (BN / 8) * BGRP;
+  static constexpr int STAGE = A_BYTES + B_BYTES;
+  static constexpr int S = (227 * 1024 - 1024) / STAGE > 5 ? 5 : (227 * 1024 - 1024) / STAGE;
+  static constexpr int OFF_BAR = S * STAGE;
+  static constexpr int SMEM = OFF_BAR + 2 * S * 8 + 16 + 128;
+  static constexpr int NCOL = 3 * BN;
+  static constexpr int COLS = NCOL <= 32 ? 32 : (NCOL <= 64 ? 64 : (NCOL <= 128 ? 128 : (NCOL <= 256 ? 256 : 512)));
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 128 && S >= 2, "tile");
+  static_assert(STAGE % 128 == 0 && AGRP % 128 == 0 && BGRP % 128 == 0, "128-byte aligned boxes");
+};
+
+// instruction descriptor of kind::f16 with both operands MN-major (transpose bits 15 and 16)
+template <int M, int N>
+__device__ __forceinline__ constexpr uint32_t instr_desc_mn() {
+  return instr_desc<M, N>() | (1u << 15) | (1u << 16);
+}
+
+template <int BN, bool SW>
+__global__ void __launch_bounds__(kTcThreads, 1) k_wgrad_tc(const __grid_constant__ ConvMaps maps, int N, int H,
+                                                           int W, int Cin, int Cout, int cps, long long nchunks,
+                                                           float* __restrict__ partial) {
+  using C = WgTcCfg<BN, SW>;
+  constexpr int S = C::S;
+  extern __shared__ char smem_raw[];
+  char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+  uint64_t* empty = full + S;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(empty + S);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;  // first channel on M and on N
+  const int co0 = SW ? n0 : m0, ci0 = SW ? m0 : n0;
+  const int mch = SW ? Cin : Cout;                        // channels on M
+  const int ky = blockIdx.z % 3, split = blockIdx.z / 3;
+  const long long c0 = (long long)split * cps;
+  const int nc = (int)(c0 < nchunks ? (nchunks - c0 < cps ? nchunks - c0 : cps) : 0);
+  const int tiles_x = W / kTcBM;
+  const int ngrp = (mch - m0) / 8 < 16 ? (mch - m0) / 8 : 16;  // A channel groups loaded
+
+  // the A channel groups at or beyond the channel count stay zero in every stage
+  constexpr int GV = C::AGRP / 16;
+  for (int i = tid; i < S * (16 - ngrp) * GV; i += kTcThreads) {
+    const int st = i / ((16 - ngrp) * GV), rem = i % ((16 - ngrp) * GV);
+    reinterpret_cast<uint4*>(smem + st * C::STAGE + ngrp * C::AGRP)[rem] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(C::COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 2 * S; ++i) mbar_init(&full[i]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (tid == 0 && nc > 0) {
+    int pend_full[S], pend_empty[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) pend_full[i] = pend_empty[i] = -1;
+    // dz boxes: 8 output channels x 128 pixels; x boxes: 8 input channels x 130 pixels of row y + ky - 1
+    const int ndz = SW ? BN / 8 : ngrp, nx = SW ? ngrp : BN / 8;
+    const unsigned tx = (unsigned)(ndz * 2048 + nx * kHaloPx * 16);
+    auto issue = [&](int c, int st) {
+      const long long g = c0 + c;
+      const int x0 = (int)(g % tiles_x) * kTcBM;
+      const long long rowg = g / tiles_x;
+      const int n = (int)(rowg / H), y = (int)(rowg % H);
+      char* As = smem + st * C::STAGE;
+      char* Bs = As + C::A_BYTES;
+      char* dzs = SW ? Bs : As;
+      char* xs = SW ? As : Bs;
+      constexpr int DZG = SW ? C::BGRP : C::AGRP, XG = SW ? C::AGRP : C::BGRP;
+      mbar_expect_tx(&full[st], tx);
+      for (int j = 0; j < ndz; ++j) tma_load_4d(dzs + j * DZG, &maps.w, co0 + 8 * j, x0, y, n, &full[st]);
+      for (int j = 0; j < nx; ++j) tma_load_4d(xs + j * XG, &maps.x, ci0 + 8 * j, x0 - 1, y + ky - 1, n, &full[st]);
+      pend_full[st] = c;
+    };
+    constexpr uint32_t idesc = instr_desc_mn<kTcBM, BN>();
+    bool ok = true;
+    for (int c = 0; c < S && c < nc; ++c) issue(c, c);
+    for (int c = 0; c < nc && ok; ++c) {
+      const int st = c % S;
+      ok = mbar_wait_ok(&full[st], (unsigned)(c / S) & 1u, true);
+      if (!ok) break;
+      pend_full[st] = -1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = smem_u32(smem + st * C::STAGE), b0 = a0 + C::A_BYTES;
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        // tap kx: the x halo window starts kx pixels (16 B each) into its boxes
+        const uint32_t ash = SW ? (uint32_t)(kx * 16) : 0u, bsh = SW ? 0u : (uint32_t)(kx * 16);
+#pragma unroll
+        for (int s8 = 0; s8 < 8; ++s8) {
+          const uint64_t ad = smem_desc(a0 + ash + s8 * 256, 128, C::AGRP);
+          const uint64_t bd = smem_desc(b0 + bsh + s8 * 256, 128, C::BGRP);
+          tc_mma(tmem + (uint32_t)(kx * BN), ad, bd, idesc, (c > 0 || s8 > 0) ? 1u : 0u);
+        }
+      }
+      tc_commit(&empty[st]);
+      pend_empty[st] = c;
+      if (c >= 1 && c - 1 + S < nc) {
+        const int ps = (c - 1) % S;
+        ok = mbar_wait_ok(&empty[ps], (unsigned)((c - 1) / S) & 1u, true);
+        if (!ok) break;
+        pend_empty[ps] = -1;
+        issue(c - 1 + S, ps);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      if (pend_full[i] >= 0) mbar_wait_ok(&full[i], (unsigned)(pend_full[i] / S) & 1u, false);
+      if (pend_empty[i] >= 0) mbar_wait_ok(&empty[i], (unsigned)(pend_empty[i] / S) & 1u, false);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  // epilogue: warp w holds channels m0 + 32 w + lane of M (TMEM lanes), BN channels of N per tap
+  const int m = m0 + warp * 32 + lane;
+  float* out = partial + (size_t)split * Cout * 9 * Cin;
+#pragma unroll 1
+  for (int kx = 0; kx < 3; ++kx) {
+    const int tap = ky * 3 + kx;
+#pragma unroll
+    for (int cc = 0; cc < BN; cc += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(kx * BN + cc), v);
+      if (nc == 0) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = 0.0f;
+      }
+      if (m < mch) {
+        if constexpr (SW) {  // m = input channel, columns = output channels n0 + cc ..
+#pragma unroll
+          for (int i = 0; i < 16; ++i) out[((size_t)(n0 + cc + i) * 9 + tap) * Cin + m] = v[i];
+        } else {             // m = output channel, columns = input channels n0 + cc ..
+          float* o = out + ((size_t)m * 9 + tap) * Cin + n0 + cc;
+#pragma unroll
+          for (int i = 0; i < 16; i += 4) *reinterpret_cast<float4*>(o + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::COLS) : "memory");
+  }
+}
+
+__global__ void k_wg_sum(const float* __restrict__ partial, int splits, size_t n, float* __restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0.0f;
+  for (int k = 0; k < splits; ++k) s += partial[(size_t)k * n + i];
+  out[i] = s;
+}
+
+// Tensor maps of the weight gradient: x (C, W, H, N) with boxes of 8
+// channels x 130 pixels x 1 row, dz (Cout, W, H, N) with boxes of 8 channels x
+// 128 pixels x 1 row (kept in ConvMaps::w).
+inline int encode_wgrad_maps(ConvMaps& m, const bf16* x, const bf16* dz, int N, int H, int W, int Cin, int Cout) {
+  const fd::EncodeTiledFn fn = fd::encode_tiled_fn();
+  FD_REQUIRE(fn != nullptr, FD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const cuuint32_t e4[4] = {1u, 1u, 1u, 1u};
+  const cuuint64_t xd[4] = {(cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+  const cuuint64_t xs[3] = {(cuuint64_t)Cin * 2, (cuuint64_t)W * Cin * 2, (cuuint64_t)H * W * Cin * 2};
+  const cuuint32_t xb[4] = {8u, (cuuint32_t)kHaloPx, 1u, 1u};
+  CUresult r = fn(&m.x, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(x), xd, xs, xb, e4,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  FD_REQUIRE(r == CUDA_SUCCESS, FD_ERR_CUDA, "sg_conv3x3_wgrad_tc: input tensor map (%d)", (int)r);
+  const cuuint64_t dd[4] = {(cuuint64_t)Cout, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+  const cuuint64_t ds[3] = {(cuuint64_t)Cout * 2, (cuuint64_t)W * Cout * 2, (cuuint64_t)H * W * Cout * 2};
+  const cuuint32_t db[4] = {8u, (cuuint32_t)kTcBM, 1u, 1u};
+  r = fn(&m.w, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(dz), dd, ds, db, e4,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  FD_REQUIRE(r == CUDA_SUCCESS, FD_ERR_CUDA, "sg_conv3x3_wgrad_tc: gradient tensor map (%d)", (int)r);
+  return FD_OK;
+}
+
+template <int BN, bool SW>
+int launch_wgrad_tc(const bf16* x, const bf16* dz, int N, int H, int W, int Cin, int Cout, float* dw, float* partial,
+                    size_t partial_floats, int splits, cudaStream_t s) {
+  using C = WgTcCfg<BN, SW>;
+  static_assert(C::SMEM <= 227 * 1024, "shared memory");
+  auto kern = k_wgrad_tc<BN, SW>;
+  static std::atomic<unsigned long long> attr_done{0};
+  if (fd::ensure_smem_attr(kern, 227 * 1024, attr_done) != cudaSuccess)
+    return fd::check_launch("sg_conv3x3_wgrad_tc: shared-memory attribute");
+  const long long nchunks = (long long)N * H * (W / kTcBM);
+  const int m_t = ((SW ? Cin : Cout) + 127) / 128, n_t = (SW ? Cout : Cin) / BN;
+  const size_t n = (size_t)Cout * 9 * Cin;
+  if (splits <= 0) {  // about two CTAs per SM, no more than the chunks or the partial buffer allow
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long per = (long long)m_t * n_t * 3;
+    splits = (int)std::max<long long>(1, (2LL * sms + per - 1) / per);
+  }
+  if ((long long)splits > nchunks) splits = (int)nchunks;
+  if ((size_t)splits * n > partial_floats) splits = (int)(partial_floats / n);
+  FD_REQUIRE(splits >= 1, FD_ERR_ARG, "sg_conv3x3_wgrad_tc: partial buffer too small");
+  const int cps = (int)((nchunks + splits - 1) / splits);
+  ConvMaps maps;
+  if (int r = encode_wgrad_maps(maps, x, dz, N, H, W, Cin, Cout)) return r;
+  dim3 grid((unsigned)m_t, (unsigned)n_t, (unsigned)(3 * splits));
+  kern<<<grid, kTcThreads, C::SMEM, s>>>(maps, N, H, W, Cin, Cout, cps, nchunks, partial);
+  k_wg_sum<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(partial, splits, n, dw);
+  return fd::check_launch("sg_conv3x3_wgrad_tc");
+}
+
 template <int BN, int BK, int R>
 int launch_tch_r(const bf16* x, int N, int H, int W, int Cin, const bf16* w, const float* b, int Cout, int act,
                  bf16* z, bf16* y, cudaStream_t s) {
@@ -1156,6 +1407,30 @@ int sg_conv3x3_tma_ws(const void* x, int N, int H, int W, int Cin, const void* w
   if (Cout % 64 == 0) return sg::launch_ws<64>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   if (Cout % 32 == 0) return sg::launch_ws<32>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
   return sg::launch_ws<16>(xb, N, H, W, Cin, wb, bias, Cout, act, zb, yb, s);
+}
+
+int sg_conv3x3_wgrad_tc(const void* x, const void* dz, int N, int H, int W, int Cin, int Cout, float* dw,
+                        float* partial, size_t partial_floats, int splits, void* stream) {
+  FD_REQUIRE(x && dz && dw && partial && N > 0 && H > 0 && W > 0, FD_ERR_ARG, "sg_conv3x3_wgrad_tc: bad arguments");
+  FD_REQUIRE(W % sg::kTcBM == 0 && Cin % 16 == 0 && Cout % 16 == 0 && Cin > 0 && Cout > 0, FD_ERR_SHAPE,
+             "sg_conv3x3_wgrad_tc: needs W a multiple of 128 and channel counts multiples of 16 (got W=%d, %d -> %d)",
+             W, Cin, Cout);
+  FD_REQUIRE(((uintptr_t)x | (uintptr_t)dz | (uintptr_t)dw | (uintptr_t)partial) % 16 == 0, FD_ERR_ARG,
+             "sg_conv3x3_wgrad_tc: tensors must be 16-byte aligned");
+  using sg::bf16;
+  cudaStream_t s = fd::as_stream(stream);
+  const bf16 *xb = (const bf16*)x, *db = (const bf16*)dz;
+  // the larger channel count on M (128 rows of the MMA), the other on N
+  if (Cin > Cout) {
+    if (Cout % 128 == 0) return sg::launch_wgrad_tc<128, true>(xb, db, N, H, W, Cin, Cout, dw, partial, partial_floats, splits, s);
+    if (Cout % 64 == 0) return sg::launch_wgrad_tc<64, true>(xb, db, N, H, W, Cin, Cout, dw, partial, partial_floats, splits, s);
+    if (Cout % 32 == 0) return sg::launch_wgrad_tc<32, true>(xb, db, N, H, W, Cin, Cout, dw, partial, partial_floats, splits, s);
+    return sg::launch_wgrad_tc<16, true>(xb, db, N, H, W, Cin, Cout, dw, partial, partial_floats, splits, s);
+  }
+  if (Cin % 128 == 0) return sg::launch_wgrad_tc<128, false>(xb, db, N, H, W, Cin, Cout, dw, partial, partial_floats, splits, s);
+  if (Cin % 64 == 0) return sg::launch_wgrad_tc<64, false>(xb, db, N, H, W, Cin, Cout, dw, partial, partial_floats, splits, s);
+  if (Cin % 32 == 0) return sg::launch_wgrad_tc<32, false>(xb, db, N, H, W, Cin, Cout, dw, partial, partial_floats, splits, s);
+  return sg::launch_wgrad_tc<16, false>(xb, db, N, H, W, Cin, Cout, dw, partial, partial_floats, splits, s);
 }
 
 int sg_tc_status(unsigned* out, int clear) {

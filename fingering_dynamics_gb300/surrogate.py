@@ -92,7 +92,9 @@ class UNet:
         "tcgen05"), "tma_ws" (its persistent warp-specialised form, same
         shapes), "mma" (warp-level tensor-core instructions) or "auto" (all
         that take the shape timed once per convolution shape at first use, the
-        fastest kept); the weight gradient always uses the warp-level kernel."""
+        fastest kept).  The weight gradient runs on the tcgen05 kernel at widths
+        that are multiples of 128 for every choice but "mma" ("auto": the faster
+        of the two per shape), else on the warp-level kernel."""
         if conv not in ("tcgen05", "tma", "tma_ws", "mma", "auto"):
             raise ValueError("conv must be 'tcgen05', 'tma', 'tma_ws', 'mma' or 'auto'")
         self.conv = conv
@@ -215,6 +217,38 @@ class UNet:
             fn = self.conv_choice[key] = best[1]
         L.call(fn, *args)
 
+    _WGRAD = {"mma": "sg_conv3x3_wgrad", "tcgen05": "sg_conv3x3_wgrad_tc"}
+
+    def _run_wgrad(self, inp, dz, N, h, w, ci, co, gw, part):
+        """Weight gradient of one layer: the tcgen05 kernel (widths that are
+        multiples of 128) or the warp-level one; with conv="auto" both are timed
+        once per shape and the faster kept (their FP32 sums differ in the last
+        bits only)."""
+        key = ("wgrad", N, h, w, ci, co)
+        args = (_p(inp), _p(dz), N, h, w, ci, co, _p(gw), _p(part), part.numel(), 0, _s())
+        ok_tc = w % 128 == 0
+        if self.conv == "mma" or not ok_tc:
+            fn = self._WGRAD["mma"]
+        elif self.conv != "auto":
+            fn = self._WGRAD["tcgen05"]
+        elif key in self.conv_choice:
+            fn = self.conv_choice[key]
+        else:
+            best = None
+            for fn in self._WGRAD.values():
+                L.call(fn, *args)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(2):
+                    L.call(fn, *args)
+                e1.record()
+                e1.synchronize()
+                t = e0.elapsed_time(e1)
+                if best is None or t < best[0]:
+                    best = (t, fn)
+            fn = self.conv_choice[key] = best[1]
+        L.call(fn, *args)
+
     def _conv(self, name, x, B, act=True):
         ci, co = self.shapes[name]
         N, h, w, c = x.shape
@@ -269,8 +303,7 @@ class UNet:
         ci, co = self.shapes[name]
         N, h, w, _ = inp.shape
         s = _s()
-        L.call("sg_conv3x3_wgrad", _p(inp), _p(dz), N, h, w, ci, co, _p(self.gw[name]), _p(B["wpart"]),
-               B["wpart"].numel(), 0, s)
+        self._run_wgrad(inp, dz, N, h, w, ci, co, self.gw[name], B["wpart"])
         L.call("sg_bias_grad", _p(dz), N * h * w, co, _p(self.gb[name]), _p(B["bpart"]), s)
         if not need_dx:
             return None

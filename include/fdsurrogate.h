@@ -65,6 +65,15 @@ int sg_flip_weights(const void* w, int Cin, int Cout, void* wt, void* stream);
 int sg_conv3x3_wgrad(const void* x, const void* dz, int N, int H, int W, int Cin, int Cout, float* dw,
                      float* partial, size_t partial_floats, int splits, void* stream);
 
+/* sg_conv3x3_wgrad on the fifth-generation tensor cores: D[co][ci] per tap
+ * with K = pixels, both operands MN-major tensor-map boxes (dz and the x halo
+ * of a kernel row), accumulators in tensor memory; the same FP32 partials
+ * added in a fixed order.  Same arguments and result; needs W a multiple of
+ * 128 and Cin, Cout multiples of 16 (FD_ERR_SHAPE otherwise); splits <= 0
+ * picks about two CTAs per SM within what `partial` holds. */
+int sg_conv3x3_wgrad_tc(const void* x, const void* dz, int N, int H, int W, int Cin, int Cout, float* dw,
+                        float* partial, size_t partial_floats, int splits, void* stream);
+
 /* Floats of `partial` that sg_conv3x3_wgrad needs with splits <= 0. */
 size_t sg_wgrad_partial_floats(int N, int H, int W, int Cin, int Cout);
 

@@ -110,6 +110,11 @@ def test_new_entry_points_check_their_arguments_on_the_host(lib):
             with pytest.raises(L.FDError) as e:
                 L.call(fn, vp(256), 1, 4, w, cin, vp(512), None, cout, act, None, vp(768), None)
             assert e.value.code == code
+        if code == -2:
+            with pytest.raises(L.FDError) as e:
+                L.call("sg_conv3x3_wgrad_tc", vp(256), vp(512), 1, 4, w, cin, cout, vp(768), vp(1024), 1 << 20, 0,
+                       None)
+            assert e.value.code == code
 
 
 def test_integration_stub_struct_matches_the_binding():

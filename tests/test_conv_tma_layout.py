@@ -166,3 +166,79 @@ def test_launch_choice_fits_shared_and_tensor_memory(pair):
     # 64-channel tiles are paired (two CTAs an SM); 128-channel tiles keep one CTA of four rows
     assert launch_choice(64, 8, 384)[:2] == (4, 2) and launch_choice(64, 8, 384)[3] == 2
     assert launch_choice(128, 8, 384)[:2] == (4, 3) and launch_choice(128, 8, 384)[3] == 1
+
+
+# ---------------------------------------------------------------------------
+# The tcgen05 weight gradient (k_wgrad_tc): both operands MN-major.
+# ---------------------------------------------------------------------------
+WG_BGRP = 2176  # bytes between the 8-channel groups of the x halo (130 pixels x 16 B, padded to 128 B)
+
+
+def operand_mn(st, start, lbo, sbo, rows):
+    """MN-major canonical layout without swizzle: element (mn, k) at start +
+    (mn // 8) * SBO + (mn % 8) * 2 + (k // 8) * LBO + (k % 8) * 16 bytes (the
+    16-byte rows of a core matrix run along MN, its eight rows along K; as for
+    K-major operands, LBO strides along K and SBO along MN, the reading the GPU
+    tests of the kernel confirm)."""
+    mn = np.arange(rows)[:, None]
+    k = np.arange(16)[None, :]
+    addr = start + (mn // 8) * sbo + (mn % 8) * 2 + (k // 8) * lbo + (k % 8) * 16
+    assert addr.min() >= 0 and addr.max() + 2 <= 2 * st.size
+    return st[addr // 2]
+
+
+def wgrad_stage(x, dz, n, y, x0, co0, ci0, ky, BN):
+    """One stage of k_wgrad_tc as its boxes fill it: A = dz boxes (8 output
+    channels x 128 pixels) for the channel groups below Cout (the others
+    zeroed once), B = x boxes (8 input channels x 130 pixels of row y+ky-1)."""
+    N, H, W, Cin = x.shape
+    Cout = dz.shape[3]
+    a_bytes = 16 * 2048
+    st = np.full((a_bytes + (BN // 8) * WG_BGRP) // 2, np.nan)
+    for j in range(16):
+        o = j * 2048 // 2
+        co = co0 + 8 * j
+        if co >= Cout:
+            st[o:o + 1024] = 0.0  # zeroed once at the start of the kernel
+            continue
+        for p in range(128):
+            st[o + p * 8:o + p * 8 + 8] = dz[n, y, x0 + p, co:co + 8]
+    yy = y + ky - 1
+    for j in range(BN // 8):
+        o = (a_bytes + j * WG_BGRP) // 2
+        ci = ci0 + 8 * j
+        for p in range(130):
+            xi = x0 - 1 + p
+            ok = 0 <= yy < H and 0 <= xi < W
+            st[o + p * 8:o + p * 8 + 8] = x[n, yy, xi, ci:ci + 8] if ok else 0.0
+    return st
+
+
+@pytest.mark.parametrize("BN,Cin,Cout", [(32, 32, 16), (16, 48, 160)])
+def test_wgrad_tc_layout_matches_direct_sum(BN, Cin, Cout):
+    rng = np.random.default_rng(3)
+    N, H, W = 1, 3, 128
+    x = rng.integers(-3, 4, size=(N, H, W, Cin)).astype(np.float64)
+    dz = rng.integers(-2, 3, size=(N, H, W, Cout)).astype(np.float64)
+    xp = np.zeros((N, H + 2, W + 2, Cin))
+    xp[:, 1:-1, 1:-1] = x
+    ref = np.zeros((Cout, 9, Cin))
+    for tap in range(9):
+        ky, kx = tap // 3, tap % 3
+        ref[:, tap] = np.einsum("nhwo,nhwc->oc", dz, xp[:, ky:ky + H, kx:kx + W])
+    a_bytes = 16 * 2048
+    for co0 in range(0, Cout, 128):
+        for ci0 in range(0, Cin, BN):
+            for ky in range(3):
+                acc = np.zeros((3, 128, BN))
+                for y in range(H):  # the chunks: one row segment of 128 pixels each
+                    st = wgrad_stage(x, dz, 0, y, 0, co0, ci0, ky, BN)
+                    for kx in range(3):
+                        for s in range(8):
+                            a = operand_mn(st, s * 256, 128, 2048, 128)
+                            b = operand_mn(st, a_bytes + kx * 16 + s * 256, 128, WG_BGRP, BN)
+                            acc[kx] += a @ b.T
+                assert np.isfinite(acc).all()
+                rows = min(128, Cout - co0)
+                for kx in range(3):
+                    np.testing.assert_array_equal(acc[kx][:rows], ref[co0:co0 + rows, ky * 3 + kx, ci0:ci0 + BN])

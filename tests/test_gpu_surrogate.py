@@ -54,6 +54,34 @@ def test_conv_forward_matches_oracle(cin, cout, act):
     assert np.abs(y.float().cpu().numpy() - yr).max() <= 1e-2 * scale
 
 
+@pytest.mark.parametrize("n,h,w,cin,cout,splits", [(2, 3, 128, 16, 32, 0), (1, 4, 128, 32, 16, 0),
+                                                   (1, 2, 256, 64, 64, 0), (2, 2, 128, 96, 32, 3),
+                                                   (1, 3, 128, 128, 144, 0), (1, 2, 128, 384, 128, 5),
+                                                   (1, 2, 128, 32, 32, 7)])
+def test_tcgen05_weight_gradient_matches_oracle(n, h, w, cin, cout, splits):
+    """The tcgen05 weight gradient (MN-major operand boxes, one kernel row of
+    taps per CTA, FP32 partials added in a fixed order) against the oracle and
+    against the warp-level kernel; covers output-channel tiles that end inside
+    the 128-row tile (144 = 128 + 16), 16 to 128 input channels per tile and
+    more splits than chunks."""
+    rng = np.random.default_rng(11 + cin + cout)
+    xh, x = _bf(rng.normal(size=(n, h, w, cin)))
+    dzh, dz = _bf(rng.normal(size=(n, h, w, cout)))
+    from fingering_dynamics_gb300 import _lib as L
+    nparts = max(int(L.lib().sg_wgrad_partial_floats(n, h, w, cin, cout)), 8 * cout * 9 * cin)
+    part = torch.empty(nparts, dtype=torch.float32, device="cuda")
+    dw = torch.empty((cout, 3, 3, cin), dtype=torch.float32, device="cuda")
+    dw2 = torch.empty_like(dw)
+    _call("sg_conv3x3_wgrad_tc", _p(x), _p(dz), n, h, w, cin, cout, _p(dw), _p(part), part.numel(), splits, None)
+    _call("sg_conv3x3_wgrad", _p(x), _p(dz), n, h, w, cin, cout, _p(dw2), _p(part), part.numel(), 0, None)
+    torch.cuda.synchronize()
+    assert _tc_status() == 0
+    dwr = U.conv3x3_wgrad(xh, dzh)
+    scale = np.abs(dwr).max()
+    assert np.abs(dw.cpu().numpy() - dwr).max() <= 1e-4 * scale
+    assert np.abs(dw.cpu().numpy() - dw2.cpu().numpy()).max() <= 1e-4 * scale
+
+
 @pytest.mark.parametrize("cin,cout", [(16, 32), (32, 16), (64, 64), (96, 32)])
 def test_conv_gradients_match_oracle(cin, cout):
     """Weight gradient (FP32, deterministic split-K) and data gradient (the
