@@ -187,35 +187,48 @@ def operand_mn(st, start, lbo, sbo, rows):
     return st[addr // 2]
 
 
-def wgrad_stage(x, dz, n, y, x0, co0, ci0, ky, BN):
-    """One stage of k_wgrad_tc as its boxes fill it: A = dz boxes (8 output
-    channels x 128 pixels) for the channel groups below Cout (the others
-    zeroed once), B = x boxes (8 input channels x 130 pixels of row y+ky-1)."""
+def wgrad_stage(x, dz, n, y, x0, m0, nn0, ky, BN, sw):
+    """One stage of k_wgrad_tc as its boxes fill it.  sw = False: A = dz boxes
+    (8 output channels x 128 pixels, groups 2048 B apart) for the groups below
+    Cout, B = x boxes (8 input channels x 130 pixels of row y+ky-1, groups
+    WG_BGRP apart); sw = True: A = the x boxes (input channels on M), B = the
+    dz boxes.  A groups at or beyond the M channel count are zeroed once."""
     N, H, W, Cin = x.shape
     Cout = dz.shape[3]
-    a_bytes = 16 * 2048
-    st = np.full((a_bytes + (BN // 8) * WG_BGRP) // 2, np.nan)
-    for j in range(16):
-        o = j * 2048 // 2
-        co = co0 + 8 * j
-        if co >= Cout:
-            st[o:o + 1024] = 0.0  # zeroed once at the start of the kernel
-            continue
+    agrp, bgrp = (WG_BGRP, 2048) if sw else (2048, WG_BGRP)
+    a_bytes = 16 * agrp
+    st = np.full((a_bytes + (BN // 8) * bgrp) // 2, np.nan)
+    yy = y + ky - 1
+
+    def put_dz(o, co):
         for p in range(128):
             st[o + p * 8:o + p * 8 + 8] = dz[n, y, x0 + p, co:co + 8]
-    yy = y + ky - 1
-    for j in range(BN // 8):
-        o = (a_bytes + j * WG_BGRP) // 2
-        ci = ci0 + 8 * j
+
+    def put_x(o, ci):
         for p in range(130):
             xi = x0 - 1 + p
             ok = 0 <= yy < H and 0 <= xi < W
             st[o + p * 8:o + p * 8 + 8] = x[n, yy, xi, ci:ci + 8] if ok else 0.0
-    return st
+
+    mch = Cin if sw else Cout
+    for j in range(16):  # A
+        o = j * agrp // 2
+        ch = m0 + 8 * j
+        if ch >= mch:
+            st[o:o + agrp // 2] = 0.0  # zeroed once at the start of the kernel
+        elif sw:
+            put_x(o, ch)
+        else:
+            put_dz(o, ch)
+    for j in range(BN // 8):  # B
+        o = (a_bytes + j * bgrp) // 2
+        (put_dz if sw else put_x)(o, nn0 + 8 * j)
+    return st, a_bytes, agrp, bgrp
 
 
-@pytest.mark.parametrize("BN,Cin,Cout", [(32, 32, 16), (16, 48, 160)])
-def test_wgrad_tc_layout_matches_direct_sum(BN, Cin, Cout):
+@pytest.mark.parametrize("BN,Cin,Cout,sw", [(32, 32, 16, False), (16, 48, 160, False), (16, 48, 16, True),
+                                            (32, 144, 32, True)])
+def test_wgrad_tc_layout_matches_direct_sum(BN, Cin, Cout, sw):
     rng = np.random.default_rng(3)
     N, H, W = 1, 3, 128
     x = rng.integers(-3, 4, size=(N, H, W, Cin)).astype(np.float64)
@@ -226,19 +239,23 @@ def test_wgrad_tc_layout_matches_direct_sum(BN, Cin, Cout):
     for tap in range(9):
         ky, kx = tap // 3, tap % 3
         ref[:, tap] = np.einsum("nhwo,nhwc->oc", dz, xp[:, ky:ky + H, kx:kx + W])
-    a_bytes = 16 * 2048
-    for co0 in range(0, Cout, 128):
-        for ci0 in range(0, Cin, BN):
+    mch, nch = (Cin, Cout) if sw else (Cout, Cin)
+    for m0 in range(0, mch, 128):
+        for nn0 in range(0, nch, BN):
             for ky in range(3):
                 acc = np.zeros((3, 128, BN))
                 for y in range(H):  # the chunks: one row segment of 128 pixels each
-                    st = wgrad_stage(x, dz, 0, y, 0, co0, ci0, ky, BN)
+                    st, a_bytes, agrp, bgrp = wgrad_stage(x, dz, 0, y, 0, m0, nn0, ky, BN, sw)
                     for kx in range(3):
+                        ash, bsh = (kx * 16, 0) if sw else (0, kx * 16)
                         for s in range(8):
-                            a = operand_mn(st, s * 256, 128, 2048, 128)
-                            b = operand_mn(st, a_bytes + kx * 16 + s * 256, 128, WG_BGRP, BN)
+                            a = operand_mn(st, ash + s * 256, 128, agrp, 128)
+                            b = operand_mn(st, a_bytes + bsh + s * 256, 128, bgrp, BN)
                             acc[kx] += a @ b.T
-                assert np.isfinite(acc).all()
-                rows = min(128, Cout - co0)
+                assert np.isfinite(acc).all()  # no operand read an unwritten byte
+                rows = min(128, mch - m0)
                 for kx in range(3):
-                    np.testing.assert_array_equal(acc[kx][:rows], ref[co0:co0 + rows, ky * 3 + kx, ci0:ci0 + BN])
+                    got = acc[kx][:rows]
+                    want = ref[m0:m0 + rows, ky * 3 + kx, nn0:nn0 + BN] if not sw else \
+                        ref[nn0:nn0 + BN, ky * 3 + kx, m0:m0 + rows].T
+                    np.testing.assert_array_equal(got, want)
