@@ -57,13 +57,13 @@ def test_conv_forward_matches_oracle(cin, cout, act):
 @pytest.mark.parametrize("n,h,w,cin,cout,splits", [(2, 3, 128, 16, 32, 0), (1, 4, 128, 32, 16, 0),
                                                    (1, 2, 256, 64, 64, 0), (2, 2, 128, 96, 32, 3),
                                                    (1, 3, 128, 128, 144, 0), (1, 2, 128, 384, 128, 5),
-                                                   (1, 2, 128, 32, 32, 7)])
+                                                   (1, 2, 128, 32, 32, 7), (1, 2, 128, 64, 96, 0)])
 def test_tcgen05_weight_gradient_matches_oracle(n, h, w, cin, cout, splits):
     """The tcgen05 weight gradient (MN-major operand boxes, one kernel row of
     taps per CTA, FP32 partials added in a fixed order) against the oracle and
-    against the warp-level kernel; covers output-channel tiles that end inside
-    the 128-row tile (144 = 128 + 16), 16 to 128 input channels per tile and
-    more splits than chunks."""
+    against the warp-level kernel; covers both assignments of M (output
+    channels, input channels), tiles that end inside the 128 rows (144 = 128 +
+    16, 96), 16 to 128 channels on N and more splits than chunks."""
     rng = np.random.default_rng(11 + cin + cout)
     xh, x = _bf(rng.normal(size=(n, h, w, cin)))
     dzh, dz = _bf(rng.normal(size=(n, h, w, cout)))
