@@ -679,7 +679,20 @@ int sg_flip_weights(const void* w, int Cin, int Cout, void* wt, void* stream) {
 
 size_t sg_wgrad_partial_floats(int N, int H, int W, int Cin, int Cout) {
   if (N <= 0 || H <= 0 || W <= 0 || Cin <= 0 || Cout <= 0) return 0;
-  return (size_t)auto_splits((long long)N * H * W, Cin, Cout) * Cout * 9 * Cin;
+  long long s = auto_splits((long long)N * H * W, Cin, Cout);
+  if (W % 128 == 0 && Cin % 16 == 0 && Cout % 16 == 0) {
+    // the tcgen05 weight gradient: the larger channel count on the MMA's 128 rows, three taps per CTA,
+    // at most two waves of one CTA per SM, no more splits than chunks of 128 pixels (sg_conv3x3_wgrad_tc)
+    const int mrows = Cin > Cout ? Cin : Cout, nch = Cin > Cout ? Cout : Cin;
+    const int bn = nch % 128 == 0 ? 128 : (nch % 64 == 0 ? 64 : (nch % 32 == 0 ? 32 : 16));
+    const long long per = (long long)((mrows + 127) / 128) * (nch / bn) * 3;
+    long long t = (2 * 152) / per;
+    if (t < 1) t = 1;
+    const long long chunks = (long long)N * H * (W / 128);
+    if (t > chunks) t = chunks;
+    if (t > s) s = t;
+  }
+  return (size_t)s * Cout * 9 * Cin;
 }
 
 int sg_conv3x3_wgrad(const void* x, const void* dz, int N, int H, int W, int Cin, int Cout, float* dw,

@@ -1275,12 +1275,12 @@ int launch_wgrad_tc(const bf16* x, const bf16* dz, int N, int H, int W, int Cin,
   const long long nchunks = (long long)N * H * (W / kTcBM);
   const int m_t = ((SW ? Cin : Cout) + 127) / 128, n_t = (SW ? Cout : Cin) / BN;
   const size_t n = (size_t)Cout * 9 * Cin;
-  if (splits <= 0) {  // about two CTAs per SM, no more than the chunks or the partial buffer allow
+  if (splits <= 0) {  // the most CTAs that fill two waves of one CTA per SM, within the chunks and the buffer
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long per = (long long)m_t * n_t * 3;
-    splits = (int)std::max<long long>(1, (2LL * sms + per - 1) / per);
+    splits = (int)std::max<long long>(1, (2LL * sms) / per);
   }
   if ((long long)splits > nchunks) splits = (int)nchunks;
   if ((size_t)splits * n > partial_floats) splits = (int)(partial_floats / n);

@@ -70,11 +70,12 @@ int sg_conv3x3_wgrad(const void* x, const void* dz, int N, int H, int W, int Cin
  * of a kernel row), accumulators in tensor memory; the same FP32 partials
  * added in a fixed order.  Same arguments and result; needs W a multiple of
  * 128 and Cin, Cout multiples of 16 (FD_ERR_SHAPE otherwise); splits <= 0
- * picks about two CTAs per SM within what `partial` holds. */
+ * picks the most CTAs that fill two waves of one per SM, within what
+ * `partial` holds. */
 int sg_conv3x3_wgrad_tc(const void* x, const void* dz, int N, int H, int W, int Cin, int Cout, float* dw,
                         float* partial, size_t partial_floats, int splits, void* stream);
 
-/* Floats of `partial` that sg_conv3x3_wgrad needs with splits <= 0. */
+/* Floats of `partial` that sg_conv3x3_wgrad and sg_conv3x3_wgrad_tc need with splits <= 0. */
 size_t sg_wgrad_partial_floats(int N, int H, int W, int Cin, int Cout);
 
 /* db[c] = sum_p dz[p][c] (FP32, fixed order; partial: sg_bias_partial_floats). */
