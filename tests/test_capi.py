@@ -129,3 +129,24 @@ def test_integration_stub_struct_matches_the_binding():
         assert ctypes.sizeof(stub) == ctypes.sizeof(ours)
         for (n, t), (_, u) in zip(stub._fields_, ours._fields_):
             assert ctypes.sizeof(t) == ctypes.sizeof(u), n
+
+
+def test_wgrad_partial_buffer_covers_both_kernels():
+    """sg_wgrad_partial_floats (a host function) sizes the FP32 partial buffer
+    for the warp-level weight gradient's splits and, at widths that are
+    multiples of 128, for the tcgen05 one's: the most CTAs that fill two waves
+    of one CTA per SM (152 SMs), three taps per CTA, the larger channel count
+    on 128 rows, no more splits than 128-pixel chunks."""
+    lib = L.lib()
+    for n, h, w, cin, cout in [(32, 256, 512, 96, 32), (32, 64, 128, 384, 128), (32, 128, 256, 64, 192),
+                               (32, 64, 128, 128, 128), (1, 2, 128, 16, 16), (2, 8, 40, 32, 32)]:
+        got = int(lib.sg_wgrad_partial_floats(n, h, w, cin, cout))
+        per_split = cout * 9 * cin
+        assert got % per_split == 0 and got >= per_split
+        if w % 128 == 0:
+            mrows, nch = max(cin, cout), min(cin, cout)
+            bn = next(b for b in (128, 64, 32, 16) if nch % b == 0)
+            per = -(-mrows // 128) * (nch // bn) * 3
+            want = max(1, min(n * h * (w // 128), (2 * 152) // per))
+            assert got >= want * per_split, (n, h, w, cin, cout, got // per_split, want)
+    assert lib.sg_wgrad_partial_floats(0, 1, 128, 16, 16) == 0
