@@ -137,6 +137,7 @@ def test_wgrad_partial_buffer_covers_both_kernels():
     multiples of 128, for the tcgen05 one's: the most CTAs that fill two waves
     of one CTA per SM (152 SMs), three taps per CTA, the larger channel count
     on 128 rows, no more splits than 128-pixel chunks."""
+    from fingering_dynamics_gb300 import _lib as L
     lib = L.lib()
     for n, h, w, cin, cout in [(32, 256, 512, 96, 32), (32, 64, 128, 384, 128), (32, 128, 256, 64, 192),
                                (32, 64, 128, 128, 128), (1, 2, 128, 16, 16), (2, 8, 40, 32, 32)]:
